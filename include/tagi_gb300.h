@@ -1,0 +1,188 @@
+/*
+ * tagi_gb300.h -- C ABI of libtagi_gb300.so, the GB300 (sm_103a) treecode
+ * convolution path of Treecode-Accelerated Green Iteration.
+ *
+ * Three groups of entry points:
+ *
+ *  1. Drop-ins with the exact signatures the reference binds through ctypes
+ *     (host pointers, copies in and out inside the call).
+ *  2. Device-pointer entry points (pointers from cudaMalloc or torch tensors,
+ *     a cudaStream_t passed as void*), including the reusable plan that keeps
+ *     the tree and lists resident across Green-iteration steps.
+ *  3. Error reporting.  Nothing in this library calls exit(); every failure
+ *     sets a thread-local code and message.
+ *
+ * Enum values (kernel, singularity, approximation, compute type) are those of
+ * 3D-GreenIteration/src/utilities/BaryTreeInterface.py:20-46:
+ *   kernel         COULOMB = 1, YUKAWA = 2
+ *   singularity    NO_SINGULARITY = 0, SKIPPING = 1, SUBTRACTION = 2
+ *   approximation  LAGRANGE = 1
+ *   computeType    PARTICLE_CLUSTER = 1
+ * Supported: COULOMB/YUKAWA, all three singularity modes (NO_SINGULARITY is
+ * treated as SKIPPING: coincident pairs are left out), LAGRANGE,
+ * PARTICLE_CLUSTER, degree 1..10.  Anything else returns TAGI_ERR_UNSUPPORTED.
+ *
+ * Precision: TAGI_PREC_MIXED (FP32 pair sums with compensated accumulation,
+ * FP64 singularity term) or TAGI_PREC_FP64.
+ */
+#ifndef TAGI_GB300_H
+#define TAGI_GB300_H
+
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+enum {
+    TAGI_OK = 0,
+    TAGI_ERR_ARG = 1,
+    TAGI_ERR_CUDA = 2,
+    TAGI_ERR_UNSUPPORTED = 3,
+    TAGI_ERR_DEVICE = 4
+};
+enum { TAGI_PREC_MIXED = 0, TAGI_PREC_FP64 = 1 };
+
+/* ---------------------------------------------------------------------- */
+/* 1. Drop-ins (host pointers).                                            */
+/* ---------------------------------------------------------------------- */
+
+/* Replaces BaryTree's BaryTreeInterface as bound in
+ * 3D-GreenIteration/src/utilities/BaryTreeInterface.py:67-72 (argtypes) and
+ * called at :140-145.  Same argument order and meaning; outputArray receives
+ * the convolution (overwritten).  If beta >= 0 it selects theta, degree and
+ * leaf sizes (project-defined map, see tagi_beta_parameters).  Precision is
+ * the library default (tagi_set_precision; TAGI_PREC_FP64 unless the
+ * environment variable TAGI_PRECISION=mixed is set).  Errors: prints one line
+ * to stderr and sets tagi_last_error(); never exits. */
+void BaryTreeInterface(int numTargets, int numSources, double *targetX, double *targetY,
+                       double *targetZ, double *targetValue, double *sourceX, double *sourceY,
+                       double *sourceZ, double *sourceValue, double *sourceWeight,
+                       double *outputArray, int kernel, int numberOfKernelParameters,
+                       double *kernelParameters, int singularity, int approximation,
+                       int computeType, double theta, int degree, int sourceLeafSize,
+                       int targetLeafSize, double sizeCheck, double beta, int verbosity);
+
+/* BaryTreeInterface with an explicit precision and a status return. */
+int tagi_BaryTreeInterface_ex(int numTargets, int numSources, const double *targetX,
+                              const double *targetY, const double *targetZ,
+                              const double *targetValue, const double *sourceX,
+                              const double *sourceY, const double *sourceZ,
+                              const double *sourceValue, const double *sourceWeight,
+                              double *outputArray, int kernel, int numberOfKernelParameters,
+                              const double *kernelParameters, int singularity, int approximation,
+                              int computeType, double theta, int degree, int sourceLeafSize,
+                              int targetLeafSize, double sizeCheck, double beta, int verbosity,
+                              int precision);
+
+/* Replaces modifiedGramSchmidt_singleWavefunction,
+ * 3D-GreenIteration/src/utilities/Orthogonalization.h:5 (Orthogonalization.c:14),
+ * bound in orthogonalization_wrapper.py:28-30.  V is row-major
+ * [numWavefunctions x numPoints]; U is orthogonalized against rows
+ * 0..targetWavefunction-1, normalized in the W inner product and written to
+ * U and to row targetWavefunction of V. */
+void modifiedGramSchmidt_singleWavefunction(double *V, double *U, double *W, int targetWavefunction,
+                                            int numPoints, int numWavefunctions);
+
+/* Replaces InterpolateBetweenTwoMeshes,
+ * 3D-GreenIteration/src/utilities/TwoMeshInterpolation.c:163-165, bound in
+ * interpolation_wrapper.py:27-31.  fineF is accumulated into, as there. */
+void InterpolateBetweenTwoMeshes(double *coarseX, double *coarseY, double *coarseZ,
+                                 double *coarseF, int *pointsPerCell_coarse, int coarseN,
+                                 double *fineX, double *fineY, double *fineZ, double *fineF,
+                                 int *pointsPerCell_fine, int fineN, int numberOfCells,
+                                 int cellOrder);
+
+/* ---------------------------------------------------------------------- */
+/* 2. Device pointers.                                                     */
+/* ---------------------------------------------------------------------- */
+
+/* One-shot treecode on device arrays (the device form of BaryTreeInterface:
+ * same parameters, BaryTreeInterface.py:140-145, plus precision and stream).
+ * Returns a status. */
+int tagi_treecode_dev(int numTargets, int numSources, const double *targetX,
+                      const double *targetY, const double *targetZ, const double *targetValue,
+                      const double *sourceX, const double *sourceY, const double *sourceZ,
+                      const double *sourceValue, const double *sourceWeight, double *outputArray,
+                      int kernel, int numberOfKernelParameters, const double *kernelParameters,
+                      int singularity, int approximation, int computeType, double theta,
+                      int degree, int sourceLeafSize, int targetLeafSize, double sizeCheck,
+                      double beta, int verbosity, int precision, void *stream);
+
+/* Reusable plan: trees, interaction lists, proxy grids and weight charges for
+ * one (targets, sources, weights) set; device inputs are read during the call
+ * only.  Corresponds to the part of one callTreedriver call
+ * (BaryTreeInterface.py:88-158) that depends on the mesh alone. */
+typedef struct tagi_plan tagi_plan;
+int tagi_plan_create(tagi_plan **plan, int numTargets, const double *targetX,
+                     const double *targetY, const double *targetZ, int numSources,
+                     const double *sourceX, const double *sourceY, const double *sourceZ,
+                     const double *sourceWeight, double theta, int degree, int sourceLeafSize,
+                     int targetLeafSize, double sizeCheck, void *stream);
+int tagi_plan_destroy(tagi_plan *plan);
+
+/* Convolve numOrbitals charge vectors over one plan in one launch sequence.
+ * targetValues [numOrbitals x numTargets], sourceValues [numOrbitals x
+ * numSources], output [numOrbitals x numTargets] (device, row-major);
+ * kernelParameters [numOrbitals x numberOfKernelParameters] on the HOST
+ * (orbital o uses kernelParameters[o * numberOfKernelParameters]).  With
+ * numOrbitals = 1 this is the per-call convolution of callTreedriver. */
+int tagi_plan_convolve(tagi_plan *plan, int numOrbitals, const double *targetValues,
+                       const double *sourceValues, double *output, int kernel,
+                       int numberOfKernelParameters, const double *kernelParameters,
+                       int singularity, int precision, void *stream);
+
+/* Plan statistics: info[0..11] = source nodes, target nodes, batches,
+ * near-list entries, far-list entries, slots, proxy points P, upward items,
+ * merged near ranges, largest batch, near pairs, far pairs (per orbital). */
+int tagi_plan_info(const tagi_plan *plan, double *info);
+
+/* Copies of the plan's integer structure to HOST arrays, for parity checks.
+ * which = 0: source tree, 1: target tree.  Array sizes from tagi_plan_info. */
+int tagi_plan_get_tree(const tagi_plan *plan, int which, uint64_t *codes, int *perm, int *begin,
+                       int *end, int *parent, int *first_child, int *nchild, double *center,
+                       double *half, double *radius);
+int tagi_plan_get_lists(const tagi_plan *plan, int *batch_node, int *near_off, int *near_list,
+                        int *far_off, int *far_list, int *slot_node);
+/* which = 0: weight charges (FP64); 1: charges of the last FP64 call;
+ * 2: charges of the last mixed call (widened).  [orbital][slot][P] to host. */
+int tagi_plan_get_charges(const tagi_plan *plan, int which, int numOrbitals, double *out);
+
+/* FP64 direct sum for the targets listed in subset (NULL = all); output[q]
+ * is the value at target subset[q].  The exact convolution. */
+int tagi_direct_dev(int numTargets, const double *targetX, const double *targetY,
+                    const double *targetZ, const double *targetValue, int numSubset,
+                    const int *subset, int numSources, const double *sourceX,
+                    const double *sourceY, const double *sourceZ, const double *sourceValue,
+                    const double *sourceWeight, double *output, int kernel,
+                    const double *kernelParameters, int singularity, void *stream);
+
+/* Device form of modifiedGramSchmidt_singleWavefunction (Orthogonalization.c:14). */
+int tagi_mgs_dev(double *V, double *U, const double *W, int targetWavefunction, int numPoints,
+                 int numWavefunctions, void *stream);
+
+/* Device form of InterpolateBetweenTwoMeshes (TwoMeshInterpolation.c:163);
+ * the points-per-cell arrays are device int32 arrays. */
+int tagi_interp_dev(const double *coarseX, const double *coarseY, const double *coarseZ,
+                    const double *coarseF, const int *pointsPerCell_coarse, int coarseN,
+                    const double *fineX, const double *fineY, const double *fineZ,
+                    double *fineF, const int *pointsPerCell_fine, int fineN, int numberOfCells,
+                    int cellOrder, void *stream);
+
+/* ---------------------------------------------------------------------- */
+/* 3. Configuration and errors.                                            */
+/* ---------------------------------------------------------------------- */
+int tagi_set_precision(int precision);   /* default for BaryTreeInterface */
+int tagi_get_precision(void);
+/* beta in [0, 1] -> theta, degree, leaf sizes (project-defined). */
+int tagi_beta_parameters(double beta, double *theta, int *degree, int *sourceLeafSize,
+                         int *targetLeafSize);
+int tagi_last_error(void);
+const char *tagi_last_error_message(void);
+void tagi_clear_error(void);
+int tagi_version(void);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* TAGI_GB300_H */

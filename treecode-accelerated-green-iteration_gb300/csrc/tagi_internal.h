@@ -1,0 +1,169 @@
+// Internal declarations shared by the CUDA translation units of libtagi_gb300.
+//
+// Data layout in HBM (one plan = one mesh / one source-target pair):
+//   sorted sources   x,y,z,w  FP64 SoA in Morton order (plus FP32 w for the
+//                    mixed path); perm maps sorted position -> caller index
+//   sorted targets   x,y,z    FP64 SoA in Morton order
+//   tree nodes       begin,end,parent,first_child,nchild (int32 SoA);
+//                    center, half (FP64, 3 per node), radius (FP64)
+//   lists            CSR per target batch: near node ids, far node ids, and
+//                    the near list merged into contiguous source ranges
+//   slots            one per far-list node: proxy geometry + modified charges
+//                    [slot][P] (P = (degree+1)^3), FP32 (mixed) or FP64
+#pragma once
+#include <cuda_runtime.h>
+#include <cstdint>
+#include <cstdio>
+#include <vector>
+
+#include "../../include/tagi_gb300.h"  // status codes TAGI_OK, TAGI_ERR_*
+
+namespace tagi {
+
+// Kernel / singularity / approximation / compute-type values are those of
+// 3D-GreenIteration/src/utilities/BaryTreeInterface.py:20-46.
+enum { KERNEL_COULOMB = 1, KERNEL_YUKAWA = 2 };
+enum { SING_NONE = 0, SING_SKIPPING = 1, SING_SUBTRACTION = 2 };
+enum { APPROX_LAGRANGE = 1 };
+enum { COMPUTE_PARTICLE_CLUSTER = 1 };
+enum { PREC_MIXED = 0, PREC_FP64 = 1 };
+
+constexpr int MAX_DEGREE = 10;        // far-field kernels are instantiated for 1..10
+constexpr int TRAVERSAL_STACK = 256;  // DFS stack entries per target batch
+
+int set_error(int code, const char *fmt, ...);
+int last_error();
+
+#define TAGI_CUDA(call)                                                                   \
+    do {                                                                                  \
+        cudaError_t e_ = (call);                                                          \
+        if (e_ != cudaSuccess)                                                            \
+            return ::tagi::set_error(::TAGI_ERR_CUDA, "%s: %s (%s:%d)", #call,      \
+                                     cudaGetErrorString(e_), __FILE__, __LINE__);         \
+    } while (0)
+
+#define TAGI_TRY(expr)                 \
+    do {                               \
+        int s_ = (expr);               \
+        if (s_ != 0) return s_;        \
+    } while (0)
+
+#define TAGI_LAUNCH_CHECK() TAGI_CUDA(cudaGetLastError())
+
+// Stream-ordered device allocations owned by a plan (freed on destroy).
+struct Arena {
+    std::vector<void *> ptrs;
+    cudaStream_t stream = nullptr;
+    template <typename T>
+    int alloc(T **p, size_t count) {
+        void *v = nullptr;
+        size_t bytes = count * sizeof(T);
+        if (bytes == 0) bytes = 16;
+        cudaError_t e = cudaMallocAsync(&v, bytes, stream);
+        if (e != cudaSuccess)
+            return set_error(TAGI_ERR_CUDA, "device allocation of %zu bytes failed: %s", bytes,
+                             cudaGetErrorString(e));
+        ptrs.push_back(v);
+        *p = static_cast<T *>(v);
+        return TAGI_OK;
+    }
+    void release() {
+        for (void *p : ptrs) cudaFreeAsync(p, stream);
+        ptrs.clear();
+    }
+};
+
+struct Tree {
+    int n = 0;
+    int nnodes = 0;
+    int nlevels = 0;
+    std::vector<int> level_start;  // host copy: node index where each BFS level begins
+    uint64_t *codes = nullptr;     // sorted Morton codes
+    int *perm = nullptr;           // sorted position -> caller index
+    double *x = nullptr, *y = nullptr, *z = nullptr;  // sorted coordinates
+    int *begin = nullptr, *end = nullptr, *parent = nullptr, *first_child = nullptr,
+        *nchild = nullptr;
+    double *center = nullptr, *half = nullptr, *radius = nullptr;
+};
+
+struct Plan {
+    int device = 0;
+    Arena arena;
+    Tree src, tgt;
+    int degree = 7, n1 = 8, P = 512;
+    double theta = 0.7, size_check = 1.0;
+    int source_leaf = 500, target_leaf = 500;
+    int nbatch = 0, max_batch = 0;
+    int *batch_node = nullptr;             // target-tree leaf of each batch
+    int *near_off = nullptr, *near_list = nullptr;
+    int *far_off = nullptr, *far_list = nullptr;
+    int near_total = 0, far_total = 0;
+    int *rng_off = nullptr;                // merged near ranges (CSR)
+    int2 *rng = nullptr;
+    int rng_total = 0;
+    int nslots = 0;
+    int *node_slot = nullptr, *slot_node = nullptr;
+    double *slot_geom = nullptr;           // [slot][6] = center xyz, proxy half xyz
+    // upward-pass work items (slot, source chunk)
+    int nitems = 0;
+    int *item_slot = nullptr, *item_begin = nullptr, *item_end = nullptr;
+    int *slot_item_off = nullptr;          // [nslots+1]
+    double *sw64 = nullptr;                // sorted source weights
+    float *sw32 = nullptr;
+    float *what32 = nullptr;               // weight modified charges [slot][P]
+    double *what64 = nullptr;
+    int *order_near = nullptr, *order_far = nullptr;   // batches, heaviest first
+    int *queue = nullptr;                  // work-queue counters (2 ints)
+    int *err_flag = nullptr;
+    double cheb[MAX_DEGREE + 1];           // cos(m pi / degree)
+    // per-convolution scratch (grown on demand)
+    size_t scratch_orbitals = 0;
+    float *q32 = nullptr;                  // [norb][ns] sorted charges f*w (FP32)
+    float *ft32 = nullptr;                 // [norb][nt] sorted target values (FP32)
+    double *q64 = nullptr;                 // [norb][ns] sorted charges f*w
+    double *f64s = nullptr;                // [norb][ns] sorted source values f
+    double *ft64 = nullptr;                // [norb][nt] sorted target values
+    double *part = nullptr;                // upward-pass partials [norb][nitems][P]
+    float *qhat32 = nullptr;               // [norb][nslots][P]
+    double *qhat64 = nullptr;
+    double *near_out = nullptr, *far_out = nullptr;  // [norb][nt] sorted order
+    float *d_kc = nullptr;                 // [norb] exp2 constants
+    double *d_kp = nullptr, *d_ss = nullptr;         // [norb] k (or a), SS factor
+    std::vector<float> h_kc;
+    std::vector<double> h_kp, h_ss;
+    std::vector<void *> scratch;           // freed on regrow / destroy
+    // statistics (host)
+    double near_pairs = 0, far_pairs = 0;  // pair interactions per orbital
+};
+
+// scan_sort.cu
+int exclusive_scan(const int *in, int *out, int n, int *d_total, Arena &ar, cudaStream_t s);
+int radix_sort_u64(uint64_t *keys, int *vals, int n, Arena &ar, cudaStream_t s);
+
+// tree.cu
+int build_tree(Tree &t, const double *x, const double *y, const double *z, int n, int leaf,
+               Arena &ar, int *err_flag, cudaStream_t s);
+int build_lists(Plan &p, cudaStream_t s);
+
+// upward.cu
+int build_weight_charges(Plan &p, cudaStream_t s);
+int modified_charges(Plan &p, int precision, int norb, cudaStream_t s);
+
+// fields.cu
+int ensure_scratch(Plan &p, int norb);
+int convolve(Plan &p, const double *tv, const double *sv, double *out, int norb, int kernel,
+             const double *kparams, int nkp, int singularity, int precision, cudaStream_t s);
+int direct_sum(int nt, const double *tx, const double *ty, const double *tz, const double *tv,
+               int nsub, const int *sub, int ns, const double *sx, const double *sy,
+               const double *sz, const double *sv, const double *sw, double *out, int kernel,
+               double kp, int singularity, int precision, cudaStream_t s);
+
+// mgs.cu / interp.cu
+int mgs_device(double *V, double *U, const double *W, int target, int npts, int nwave,
+               cudaStream_t s);
+int interp_device(const double *cX, const double *cY, const double *cZ, const double *cF,
+                  const int *ppc_c, int coarseN, const double *fX, const double *fY,
+                  const double *fZ, double *fF, const int *ppc_f, int fineN, int ncells,
+                  int order, const int *h_ppc_c, const int *h_ppc_f, cudaStream_t s);
+
+}  // namespace tagi
