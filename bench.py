@@ -1,0 +1,417 @@
+#!/usr/bin/env python
+"""Benchmark of the GB300 treecode convolution path.
+
+Workload (default): the Coulomb Hartree convolution with singularity
+subtraction on a seeded synthetic ~1.5M-point mesh (4 nuclei in a 6 Bohr box,
+Z from {1,6,8}, order-7 cells, depth <= 7; density = 3 Gaussians per nucleus,
+exponents log-uniform in [0.1, 10]), mixed precision, degree 7, theta 0.7.
+
+One step = one full treecode convolution as one callTreedriver call does it:
+tree + batches + lists + weight charges (the plan), modified charges, near
+and far fields, epilogue -- inputs already resident in HBM.  ``value`` =
+convolutions/s over all ranks.  ``e2e`` = the same through the C ABI
+(tagi_BaryTreeInterface_ex) with pinned host buffers: host->device copies,
+device allocation and the device->host result copy are inside the timing.
+
+  python bench.py [--gpus N] [--steps K] [--warmup W] [--impl gb300|reference]
+                  [--workload hartree|orbitals]
+
+``--impl reference`` times the CPU FP64 restatement of the same treecode (the
+reference's BaryTree is not available) on the host cores, on a bounded sample
+of target batches per step, extrapolated by pair count.
+"""
+import argparse
+import ctypes
+import importlib
+import json
+import os
+import statistics
+import subprocess
+import sys
+import tempfile
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+PKG = "treecode-accelerated-green-iteration_gb300"
+sys.path.insert(0, ROOT)
+
+METRIC = "orbital convs/s at 1e-6 rel err; wall time to 1e-5 Ha SCF: chosen vs plain"
+UNIT = "convolutions/s"
+THETA, DEGREE = 0.7, 7
+LEAF = {"hartree": (2000, 2000), "orbitals": (2000, 2000)}
+PAIR_FLOPS = {"coulomb_ss": 14, "yukawa_ss": 15}  # FP32 pipe ops counted per pair (see DESIGN)
+
+
+def parse():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=5)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
+    ap.add_argument("--workload", default="hartree", choices=["hartree", "orbitals"])
+    ap.add_argument("--cpu-seconds", type=float, default=15.0,
+                    help="target CPU seconds of field work per CPU-baseline sample")
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    return ap.parse_args()
+
+
+def dist_env():
+    ws = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return ws, rank, local
+
+
+# ---------------------------------------------------------------------------
+# Workloads
+# ---------------------------------------------------------------------------
+def make_workload(name):
+    pkg = importlib.import_module(PKG)
+    syn = pkg.synthetic
+    BT = pkg.BaryTreeInterface
+    if name == "hartree":
+        mesh, rho = syn.hartree_system(seed=2)
+        return dict(mesh=mesh, values=rho[None, :], kparams=np.array([[1.0]]),
+                    kernel=BT.Kernel.COULOMB, singularity=BT.Singularity.SUBTRACTION,
+                    label="coulomb_ss", desc="coulomb_hartree_ss_1.5M")
+    mesh, F, k = syn.multi_orbital_system(seed=3, n_orb=32)
+    return dict(mesh=mesh, values=F, kparams=k[:, None], kernel=BT.Kernel.YUKAWA,
+                singularity=BT.Singularity.SUBTRACTION, label="yukawa_ss",
+                desc="yukawa_32_orbitals_1M")
+
+
+# ---------------------------------------------------------------------------
+# Clock sampling during the timed region
+# ---------------------------------------------------------------------------
+class ClockSampler:
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, gpu_index):
+        self.gpu = gpu_index
+        self.proc = None
+        self.file = None
+
+    def __enter__(self):
+        try:
+            self.file = tempfile.NamedTemporaryFile("w+", suffix=".csv", delete=False)
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", f"--id={self.gpu}", f"--query-gpu={self.FIELDS}",
+                 "--format=csv,noheader,nounits", "-lms", "200"], stdout=self.file,
+                stderr=subprocess.DEVNULL)
+        except OSError:
+            self.proc = None
+        time.sleep(0.3)
+        return self
+
+    def __exit__(self, *exc):
+        if self.proc is not None:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except subprocess.TimeoutExpired:
+                self.proc.kill()
+
+    def summary(self):
+        if self.proc is None or self.file is None:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        self.file.flush()
+        rows = []
+        with open(self.file.name) as f:
+            for line in f:
+                p = [x.strip() for x in line.split(",")]
+                if len(p) >= 9:
+                    rows.append(p)
+        os.unlink(self.file.name)
+        if not rows:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["no samples"]}
+
+        def num(x):
+            try:
+                return float(x)
+            except ValueError:
+                return None
+        sm = [num(r[1]) for r in rows if num(r[1]) is not None]
+        mx = [num(r[2]) for r in rows if num(r[2]) is not None]
+        names = ("hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap")
+        reasons = sorted({n for r in rows for n, v in zip(names, r[5:9]) if v.lower() == "active"})
+        return {"sm_mhz": statistics.median(sm) if sm else None,
+                "sm_max_mhz": max(mx) if mx else None, "reasons": reasons,
+                "samples": len(rows),
+                "power_w_max": max((num(r[3]) or 0.0) for r in rows)}
+
+
+# ---------------------------------------------------------------------------
+# CPU baseline: the FP64 treecode restatement on the host cores
+# ---------------------------------------------------------------------------
+def cpu_treecode_sample(wl, target_seconds, threads):
+    """Build the CPU plan (timed), convolve a sample of whole target batches
+    sized to ~target_seconds of field work, extrapolate to one convolution by
+    the pair counts of the full lists.  Returns (seconds per convolution, info)."""
+    from oracle import oracle as O
+    O.build()
+    mesh = wl["mesh"]
+    sl, tl = LEAF["hartree"]
+    t0 = time.perf_counter()
+    plan = O.Plan(mesh.x, mesh.y, mesh.z, mesh.x, mesh.y, mesh.z, mesh.w, THETA, DEGREE, sl, tl, 1.0)
+    t_plan = time.perf_counter() - t0
+    L = plan.lists()
+    st, tt = plan.tree(0), plan.tree(1)
+    nb = plan.n_batches
+    bsz = tt["end"][L["batch_node"]] - tt["begin"][L["batch_node"]]
+    ncnt = np.zeros(nb)
+    src_len = st["end"] - st["begin"]
+    for b in range(nb):
+        ncnt[b] = src_len[L["near_list"][L["near_off"][b]:L["near_off"][b + 1]]].sum()
+    pairs_b = bsz * (ncnt + np.diff(L["far_off"]) * plan.P)
+    total_pairs = pairs_b.sum()
+    rng = np.random.default_rng(17)
+    order = rng.permutation(nb)
+    q = wl["values"][0]
+    kp = wl["kparams"][0]
+    # calibration on a few batches, then a sample sized to the time target
+    sel = np.sort(order[:4])
+    _, (t_up, t_f), (pn, pf) = O.convolve_batches(plan, q, q, mesh.w, wl["kernel"], kp,
+                                                  wl["singularity"], sel, threads)
+    rate = (pn + pf) / max(t_f, 1e-9)
+    want = rate * target_seconds
+    csum = np.cumsum(pairs_b[order])
+    nsel = int(np.clip(np.searchsorted(csum, want) + 1, 4, nb))
+    sel = np.sort(order[:nsel])
+    _, (t_up, t_f), (pn, pf) = O.convolve_batches(plan, q, q, mesh.w, wl["kernel"], kp,
+                                                  wl["singularity"], sel, threads)
+    frac = (pn + pf) / total_pairs
+    seconds = t_plan + t_up + t_f / frac
+    return seconds, dict(batches=int(nsel), of_batches=int(nb), pair_fraction=float(frac),
+                         plan_s=t_plan, upward_s=t_up, sample_field_s=t_f,
+                         pairs_per_s=(pn + pf) / t_f)
+
+
+def reference_arm(args):
+    ws, rank, local = dist_env()
+    if rank != 0:
+        return 0
+    wl = make_workload(args.workload)
+    threads = os.cpu_count() or 1
+    per_step = max(2.0, args.cpu_seconds / 4)
+    for _ in range(args.warmup):
+        cpu_treecode_sample(wl, per_step, threads)
+    secs, info = [], None
+    t0 = time.perf_counter()
+    for _ in range(args.steps):
+        s, info = cpu_treecode_sample(wl, per_step, threads)
+        secs.append(s)
+    wall = time.perf_counter() - t0
+    mean_s = float(np.mean(secs))
+    value = 1.0 / mean_s
+    sample = (f"FP64 treecode restatement (oracle/tagi_oracle.c, OpenMP) on {info['batches']} of "
+              f"{info['of_batches']} target batches per step ({info['pair_fraction']:.4f} of the "
+              "pairs), plan + upward pass timed in full, fields extrapolated by pair count")
+    line = {"impl": "reference", "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": 0,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": mean_s * 1e3,
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+            "data": "synthetic (seeded)",
+            "config": {"workload": wl["desc"], "points": int(wl["mesh"].n), "theta": THETA,
+                       "degree": DEGREE, "leaf": list(LEAF["hartree"]), "precision": "fp64"},
+            "cpu_baseline": {"value": value, "unit": UNIT, "cores": threads, "kind": "port",
+                             "sample": sample},
+            "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+            "wall_s": wall, "cpu_pairs_per_s": info["pairs_per_s"]}
+    print(json.dumps(line), flush=True)
+    return 0
+
+
+# ---------------------------------------------------------------------------
+# GB300 arm
+# ---------------------------------------------------------------------------
+def profile_traffic(label):
+    """DRAM bytes per launch of the dominant kernel from the committed ncu summary."""
+    path = os.path.join(ROOT, "profiles", f"near_field_{label}_1.5M.md")
+    if not os.path.exists(path):
+        return None
+    for line in open(path):
+        if line.startswith("dram_bytes_per_launch"):
+            try:
+                return float(line.split("=")[1].split()[0])
+            except (IndexError, ValueError):
+                return None
+    return None
+
+
+def gb300_arm(args):
+    import torch
+    import torch.distributed as dist
+
+    ws, rank, local = dist_env()
+    torch.cuda.set_device(local)
+    if ws > 1:
+        dist.init_process_group("nccl", device_id=torch.device("cuda", local))
+    pkg = importlib.import_module(PKG)
+    dev = importlib.import_module(PKG + ".device")
+    nat = pkg._native
+    L = nat.lib()
+    wl = make_workload(args.workload)
+    mesh = wl["mesh"]
+    cuda = torch.device("cuda", local)
+    t = lambda a: torch.as_tensor(np.ascontiguousarray(a), dtype=torch.float64, device=cuda)
+    x, y, z, w = t(mesh.x), t(mesh.y), t(mesh.z), t(mesh.w)
+    vals = t(wl["values"])
+    norb = vals.shape[0]
+    sl, tl = LEAF[args.workload]
+    stream = torch.cuda.current_stream()
+
+    def step():
+        plan = dev.TreecodePlan.for_mesh(x, y, z, w, theta=THETA, degree=DEGREE, source_leaf=sl,
+                                         target_leaf=tl)
+        out = plan.convolve(vals, vals, wl["kernel"], wl["kparams"], wl["singularity"],
+                            precision="mixed")
+        info = plan.info()
+        plan.close()
+        return out, info
+
+    for _ in range(args.warmup):
+        out, info = step()
+    torch.cuda.synchronize()
+    flush = torch.empty(64 * 1024 * 1024, dtype=torch.float32, device=cuda)  # 256 MB > L2
+    evs = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True))
+           for _ in range(args.steps)]
+    L.tagi_profile(1)
+    prof_ms = np.zeros(6)
+    prof_n = np.zeros(6, dtype=np.int64)
+    prof_np = prof_n.ctypes.data_as(ctypes.POINTER(ctypes.c_longlong))
+    L.tagi_profile_read(nat.dptr(prof_ms), prof_np, 6)  # discard warm-up marks
+    with ClockSampler(local) as clocks:
+        if ws > 1:
+            dist.barrier()
+        torch.cuda.synchronize()
+        n0 = L.tagi_launch_count()
+        for k in range(args.steps):
+            flush.zero_()
+            evs[k][0].record(stream)
+            out, info = step()
+            evs[k][1].record(stream)
+        torch.cuda.synchronize()
+        if ws > 1:
+            dist.barrier()
+        launches = L.tagi_launch_count() - n0
+    L.tagi_profile_read(nat.dptr(prof_ms), prof_np, 6)
+    L.tagi_profile(0)
+    step_ms = [a.elapsed_time(b) for a, b in evs]
+    total_ms = float(sum(step_ms))
+    if ws > 1:
+        tt = torch.tensor([total_ms], device=cuda)
+        dist.all_reduce(tt, op=dist.ReduceOp.MAX)
+        total_ms = float(tt.item())
+    convs = norb * args.steps * ws
+    value = convs / (total_ms * 1e-3)
+
+    if rank != 0:
+        if ws > 1:
+            dist.destroy_process_group()
+        return 0
+
+    # accuracy of the timed result against the exact FP64 direct sum (GPU) on seeded targets
+    rng = np.random.default_rng(99)
+    sub = torch.as_tensor(np.sort(rng.choice(mesh.n, 4096, replace=False)).astype(np.int32),
+                          device=cuda)
+    o0 = out[0].contiguous()
+    ref = dev.direct(x, y, z, vals[0].contiguous(), x, y, z, vals[0].contiguous(), w, wl["kernel"],
+                     wl["kparams"][0], wl["singularity"], subset=sub)
+    rel = float(torch.linalg.norm(o0[sub.long()] - ref) / torch.linalg.norm(ref))
+
+    # roofline of the dominant field kernel
+    pairs_near, pairs_far = info["near_pairs"] * norb, info["far_pairs"] * norb
+    near_ms = prof_ms[3] / max(prof_n[3], 1)
+    far_ms = prof_ms[4] / max(prof_n[4], 1)
+    dominant = "near" if near_ms >= far_ms else "far"
+    k_ms = near_ms if dominant == "near" else far_ms
+    k_pairs = pairs_near if dominant == "near" else pairs_far
+    achieved = k_pairs / (k_ms * 1e-3)
+    peak = ctypes.c_double()
+    kp0 = float(wl["kparams"][0][0])
+    nat.check(L.tagi_pair_peak(int(wl["kernel"]), int(wl["singularity"]),
+                               0 if dominant == "near" else 1, kp0, ctypes.byref(peak),
+                               ctypes.c_void_p(stream.cuda_stream)))
+    traffic = profile_traffic(wl["label"]) if dominant == "near" else None
+    roofline = {"bound": "mufu", "achieved": achieved / 1e9, "peak": peak.value / 1e9,
+                "unit": "Gpair/s", "frac": achieved / peak.value, "traffic": traffic,
+                "kernel": f"{dominant}_mixed ({wl['label']})",
+                "peak_source": "tagi_pair_peak: same pair arithmetic, operands in shared "
+                               "memory/registers, measured live on this GPU",
+                "kernel_ms_per_launch": k_ms, "pairs_per_launch": k_pairs,
+                "fp32_tflops": achieved * PAIR_FLOPS[wl["label"]] / 1e12}
+
+    # end to end through the C ABI with pinned host buffers
+    pinned = [torch.empty(mesh.n, dtype=torch.float64, pin_memory=True) for _ in range(9)]
+    for p_, a_ in zip(pinned, (mesh.x, mesh.y, mesh.z, wl["values"][0], mesh.x, mesh.y, mesh.z,
+                               wl["values"][0], mesh.w)):
+        p_.numpy()[:] = a_
+    hout = torch.empty(mesh.n, dtype=torch.float64, pin_memory=True)
+    hp = [nat.dptr(p_.numpy()) for p_ in pinned]
+    kpar = np.ascontiguousarray(wl["kparams"][0], dtype=np.float64)
+
+    def e2e_call():
+        return L.tagi_BaryTreeInterface_ex(mesh.n, mesh.n, *hp, nat.dptr(hout.numpy()),
+                                           int(wl["kernel"]), len(kpar), nat.dptr(kpar),
+                                           int(wl["singularity"]), 1, 1, THETA, DEGREE, sl, tl,
+                                           1.0, -1.0, 0, nat.PREC_MIXED)
+    nat.check(e2e_call())
+    e2e_steps = max(1, min(args.steps, 3))
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    for _ in range(e2e_steps):
+        flush.zero_()
+        torch.cuda.synchronize()
+        nat.check(e2e_call())
+    e2e_s = (time.perf_counter() - t0) / e2e_steps
+    e2e = {"value": 1.0 / e2e_s, "unit": UNIT, "h2d_bytes_per_step": 9 * 8 * mesh.n,
+           "d2h_bytes_per_step": 8 * mesh.n, "path": "tagi_BaryTreeInterface_ex (C ABI, host buffers)",
+           "note": "per step one single-charge-vector call"}
+
+    cpu = None
+    if not args.no_cpu_baseline and ws == 1:
+        threads = os.cpu_count() or 1
+        secs, cinfo = cpu_treecode_sample(wl, args.cpu_seconds, threads)
+        cpu = {"value": norb / secs if args.workload == "hartree" else 1.0 / secs, "unit": UNIT,
+               "cores": threads, "kind": "port",
+               "sample": (f"FP64 treecode restatement on {cinfo['batches']} of {cinfo['of_batches']} "
+                          f"target batches ({cinfo['pair_fraction']:.4f} of the pairs), plan and "
+                          "upward pass timed in full, fields extrapolated by pair count")}
+
+    clk = clocks.summary()
+    line = {
+        "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": ws, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": total_ms / args.steps, "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f32+f64",
+        "data": "synthetic (seeded mesh and densities)",
+        "config": {"workload": wl["desc"], "points": int(mesh.n), "orbitals": int(norb),
+                   "theta": THETA, "degree": DEGREE, "leaf": [sl, tl], "precision": "mixed",
+                   "step": "plan (tree, lists, weight charges) + convolution, inputs in HBM",
+                   "l2": "256 MB buffer written between timed steps (untimed)",
+                   "parallelism": f"replicas x{ws} (independent convolutions, no collective)",
+                   "rel_l2_vs_fp64_direct": rel, "rel_l2_sample_targets": 4096,
+                   "pairs_per_conv": info["near_pairs"] + info["far_pairs"],
+                   "near_pairs": info["near_pairs"], "far_pairs": info["far_pairs"]},
+        "phase_ms_per_step": {k: float(v) / args.steps for k, v in zip(
+            ("tree", "lists", "upward", "near", "far", "glue"), prof_ms)},
+        "roofline": roofline, "cpu_baseline": cpu, "e2e": e2e, "clocks": clk,
+        "gpu_launches": int(launches),
+    }
+    print(json.dumps(line), flush=True)
+    if ws > 1:
+        dist.destroy_process_group()
+    return 0
+
+
+def main():
+    args = parse()
+    if args.impl == "reference":
+        return reference_arm(args)
+    return gb300_arm(args)
+
+
+if __name__ == "__main__":
+    sys.exit(main())

@@ -144,9 +144,11 @@ int tagi_plan_get_tree(const tagi_plan *plan, int which, uint64_t *codes, int *p
                        double *half, double *radius);
 int tagi_plan_get_lists(const tagi_plan *plan, int *batch_node, int *near_off, int *near_list,
                         int *far_off, int *far_list, int *slot_node);
-/* which = 0: weight charges (FP64); 1: charges of the last FP64 call;
- * 2: charges of the last mixed call (widened).  [orbital][slot][P] to host. */
-int tagi_plan_get_charges(const tagi_plan *plan, int which, int numOrbitals, double *out);
+/* which = 0: weight charges (FP64, built here if no FP64 call built them);
+ * 1: charges of the last FP64 call; 2: charges of the last mixed call;
+ * 3: weight charges of the mixed path.  [orbital][slot][P] to host, widened
+ * to double. */
+int tagi_plan_get_charges(tagi_plan *plan, int which, int numOrbitals, double *out);
 
 /* FP64 direct sum for the targets listed in subset (NULL = all); output[q]
  * is the value at target subset[q].  The exact convolution. */
@@ -177,6 +179,22 @@ int tagi_get_precision(void);
 /* beta in [0, 1] -> theta, degree, leaf sizes (project-defined). */
 int tagi_beta_parameters(double beta, double *theta, int *degree, int *sourceLeafSize,
                          int *targetLeafSize);
+/* Instrumentation: number of kernels this library has launched in this
+ * process; optional per-phase device timing with CUDA events on the
+ * launching stream.  Phases: 0 tree, 1 lists, 2 upward pass, 3 near field,
+ * 4 far field, 5 glue.  tagi_profile_read waits for the recorded events,
+ * returns summed milliseconds and mark counts per phase (nphase >= 6), and
+ * clears the record. */
+long long tagi_launch_count(void);
+/* Pair-throughput ceiling of the mixed-precision field kernels on this GPU:
+ * their inner-loop arithmetic (variant 0: near-field loop, 1: far-field
+ * proxy-grid loop) with operands in shared memory and registers and no
+ * global-memory traffic, timed with CUDA events.  Pair interactions / s. */
+int tagi_pair_peak(int kernel, int singularity, int variant, double kernelParameter,
+                   double *pairsPerSecond, void *stream);
+int tagi_profile(int enable);
+int tagi_profile_read(double *ms, long long *count, int nphase);
+
 int tagi_last_error(void);
 const char *tagi_last_error_message(void);
 void tagi_clear_error(void);

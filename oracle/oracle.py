@@ -62,6 +62,9 @@ def lib():
         L.oracle_plan_weight_charges.argtypes = [ctypes.c_void_p, _dp]
         L.oracle_plan_convolve.argtypes = [ctypes.c_void_p, _dp, _dp, _dp, ctypes.c_int, _dp,
                                            ctypes.c_int, _dp, ctypes.c_int]
+        L.oracle_plan_convolve_batches.argtypes = [ctypes.c_void_p, _dp, _dp, _dp, ctypes.c_int, _dp,
+                                                   ctypes.c_int, _dp, ctypes.c_int, ctypes.c_int,
+                                                   _ip, _dp, _dp]
         L.oracle_mgs.argtypes = [_dp, _dp, _dp, ctypes.c_int, ctypes.c_int, ctypes.c_int]
         L.oracle_interp.argtypes = [_dp, _dp, _dp, _dp, _ip, ctypes.c_int, _dp, _dp, _dp, _dp,
                                     _ip, ctypes.c_int, ctypes.c_int, ctypes.c_int]
@@ -164,6 +167,20 @@ class Plan:
         lib().oracle_plan_convolve(self.h, _p(tv), _p(sv), _p(sw), int(kernel), _p(kp),
                                    int(singularity), _p(out), nthreads)
         return out
+
+
+def convolve_batches(plan, tv, sv, sw, kernel, kparams, singularity, batches, nthreads=0):
+    """Convolve only the listed batches; returns (out, (t_upward, t_fields), (near, far pairs))."""
+    tv, sv, sw = _c(tv), _c(sv), _c(sw)
+    kp = _c(np.atleast_1d(kparams))
+    sel = _c(batches, np.int32)
+    out = np.zeros(plan.nt)
+    times = np.zeros(2)
+    pairs = np.zeros(2)
+    lib().oracle_plan_convolve_batches(plan.h, _p(tv), _p(sv), _p(sw), int(kernel), _p(kp),
+                                       int(singularity), _p(out), nthreads, len(sel), _p(sel, _ip),
+                                       _p(times), _p(pairs))
+    return out, tuple(times), tuple(pairs)
 
 
 def mgs(V, U, W, target):

@@ -520,18 +520,32 @@ void oracle_plan_weight_charges(void *vp, double *what)
     memcpy(what, p->what, sizeof(double) * (size_t)P * p->nslots);
 }
 
+static double wall_s(void)
+{
+#ifdef _OPENMP
+    return omp_get_wtime();
+#else
+    return 0.0;
+#endif
+}
+
 /*
- * Full FP64 treecode convolution.  tv, sv, sw in original order; out in
- * original target order.  phi_i = near(direct) + far(proxy) + SS term.
+ * FP64 treecode convolution for the batches listed in sel[0..nsel) (all
+ * batches when sel == NULL).  tv, sv, sw in original order; out in original
+ * target order (only the selected batches' targets are written).
+ * phi_i = near(direct) + far(proxy) + SS term.  times[0] = upward pass s,
+ * times[1] = field s; pairs[0] = near pairs, pairs[1] = far pairs (selected).
  */
-void oracle_plan_convolve(void *vp, const double *tv, const double *sv, const double *sw,
-                          int kernel, const double *kparams, int sing, double *out,
-                          int nthreads)
+void oracle_plan_convolve_batches(void *vp, const double *tv, const double *sv, const double *sw,
+                                  int kernel, const double *kparams, int sing, double *out,
+                                  int nthreads, int nsel, const int *sel, double *times,
+                                  double *pairs)
 {
     oplan *p = (oplan *)vp;
     const otree *s = &p->src, *t = &p->tgt;
     int ns = s->n, n1 = p->degree + 1, P = n1 * n1 * n1;
     double kp = kparams[0];
+    double t0 = wall_s();
     double *qs = (double *)malloc(sizeof(double) * ns);
     double *ws = (double *)malloc(sizeof(double) * ns);
     double *fs = (double *)malloc(sizeof(double) * ns);
@@ -547,15 +561,25 @@ void oracle_plan_convolve(void *vp, const double *tv, const double *sv, const do
 #pragma omp parallel for schedule(dynamic, 1)
 #endif
     for (int sl = 0; sl < p->nslots; sl++) p2m(p, sl, qs, qhat + (size_t)sl * P);
+    double t1 = wall_s();
 
     double tn[32];
     cheb2_nodes(p->degree, tn);
     int sing_ss = (sing == S_SUBTRACTION);
+    int nrun = sel ? nsel : p->nbatch;
+    double npairs = 0.0, fpairs = 0.0;
 #ifdef _OPENMP
-#pragma omp parallel for schedule(dynamic, 1)
+#pragma omp parallel for schedule(dynamic, 1) reduction(+ : npairs, fpairs)
 #endif
-    for (int b = 0; b < p->nbatch; b++) {
+    for (int bi = 0; bi < nrun; bi++) {
+        int b = sel ? sel[bi] : bi;
         int bn = p->batch_node[b];
+        int nb = t->end[bn] - t->begin[bn];
+        for (int e = p->near_off[b]; e < p->near_off[b + 1]; e++) {
+            int c = p->near_list[e];
+            npairs += (double)nb * (double)(s->end[c] - s->begin[c]);
+        }
+        fpairs += (double)nb * (double)(p->far_off[b + 1] - p->far_off[b]) * (double)P;
         for (int i = t->begin[bn]; i < t->end[bn]; i++) {
             int oi = t->perm[i];
             double xi = t->x[i], yi = t->y[i], zi = t->z[i], fi = tv[oi];
@@ -596,7 +620,18 @@ void oracle_plan_convolve(void *vp, const double *tv, const double *sv, const do
             out[oi] = acc + ss_term(kernel, sing, kp, fi);
         }
     }
+    double t2 = wall_s();
+    if (times) { times[0] = t1 - t0; times[1] = t2 - t1; }
+    if (pairs) { pairs[0] = npairs; pairs[1] = fpairs; }
     free(qs); free(ws); free(fs); free(qhat);
+}
+
+void oracle_plan_convolve(void *vp, const double *tv, const double *sv, const double *sw,
+                          int kernel, const double *kparams, int sing, double *out,
+                          int nthreads)
+{
+    oracle_plan_convolve_batches(vp, tv, sv, sw, kernel, kparams, sing, out, nthreads, 0, NULL,
+                                 NULL, NULL);
 }
 
 /* ------------------------------------------------------------------------ */

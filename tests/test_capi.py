@@ -13,7 +13,7 @@ from conftest import ROOT
 def declared_functions():
     src = open(os.path.join(ROOT, "include", "tagi_gb300.h")).read()
     src = re.sub(r"/\*.*?\*/", "", src, flags=re.S)
-    names = re.findall(r"^\s*(?:void|int|const char \*|double)\s*\*?\s*(\w+)\s*\(", src, flags=re.M)
+    names = re.findall(r"^\s*(?:void|int|long long|const char \*|double)\s*\*?\s*(\w+)\s*\(", src, flags=re.M)
     return sorted(set(names))
 
 

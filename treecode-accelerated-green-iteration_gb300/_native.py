@@ -45,6 +45,10 @@ SIGNATURES = {
     "tagi_set_precision": (_i, [_i]),
     "tagi_get_precision": (_i, []),
     "tagi_beta_parameters": (_i, [_d, _dp, _ip, _ip, _ip]),
+    "tagi_launch_count": (ctypes.c_longlong, []),
+    "tagi_pair_peak": (_i, [_i, _i, _i, _d, _dp, _vp]),
+    "tagi_profile": (_i, [_i]),
+    "tagi_profile_read": (_i, [_dp, ctypes.POINTER(ctypes.c_longlong), _i]),
     "tagi_last_error": (_i, []),
     "tagi_last_error_message": (ctypes.c_char_p, []),
     "tagi_clear_error": (None, []),

@@ -146,12 +146,16 @@ int plan_create(Plan **out, int nt, const double *tx, const double *ty, const do
     do {
         if ((rc = p->arena.alloc(&p->queue, 2)) || (rc = p->arena.alloc(&p->err_flag, 1))) break;
         cudaMemsetAsync(p->err_flag, 0, sizeof(int), s);
+        phase_mark(PH_TREE, true, s);
         if ((rc = build_tree(p->src, sx, sy, sz, ns, sl, p->arena, p->err_flag, s))) break;
         if ((rc = build_tree(p->tgt, tx, ty, tz, nt, tl, p->arena, p->err_flag, s))) break;
+        phase_mark(PH_TREE, false, s);
+        phase_mark(PH_LISTS, true, s);
         if ((rc = p->arena.alloc(&p->sw64, ns)) || (rc = p->arena.alloc(&p->sw32, ns))) break;
-        gather_weights<<<(ns + 255) / 256, 256, 0, s>>>(sw, p->src.perm, ns, p->sw64, p->sw32);
+        launch(gather_weights, (ns + 255) / 256, 256, 0, s, sw, p->src.perm, ns, p->sw64, p->sw32);
         if ((rc = build_lists(*p, s))) break;
         if ((rc = build_weight_charges(*p, s))) break;
+        phase_mark(PH_LISTS, false, s);
         cudaError_t e = cudaStreamSynchronize(s);
         if (e != cudaSuccess) { rc = set_error(TAGI_ERR_CUDA, "plan build: %s", cudaGetErrorString(e)); break; }
     } while (0);
@@ -187,7 +191,7 @@ int treecode_device(int nt, int ns, const double *tx, const double *ty, const do
     TAGI_TRY(validate_kparam(kernel, sing, kp[0]));
     if (nt == 0) return TAGI_OK;
     if (ns == 0) {
-        ss_only<<<(nt + 255) / 256, 256, 0, s>>>(tv, nt, ss_constant(kernel, sing, kp[0]), out);
+        launch(ss_only, (nt + 255) / 256, 256, 0, s, tv, nt, ss_constant(kernel, sing, kp[0]), out);
         TAGI_LAUNCH_CHECK();
         return TAGI_OK;
     }
@@ -417,13 +421,21 @@ int tagi_plan_get_lists(const tagi_plan *plan, int *batch_node, int *near_off, i
     return TAGI_OK;
 }
 
-int tagi_plan_get_charges(const tagi_plan *plan, int which, int numOrbitals, double *out) {
+int tagi_plan_get_charges(tagi_plan *plan, int which, int numOrbitals, double *out) {
     if (!plan || !out) return set_error(TAGI_ERR_ARG, "null pointer");
-    const Plan &p = *reinterpret_cast<const Plan *>(plan);
+    Plan &p = *reinterpret_cast<Plan *>(plan);
     const size_t per = (size_t)p.nslots * p.P;
     TAGI_CUDA(cudaDeviceSynchronize());
     if (which == 0) {
+        TAGI_TRY(ensure_weight_charges64(p, p.arena.stream));
+        TAGI_CUDA(cudaDeviceSynchronize());
         TAGI_CUDA(cudaMemcpy(out, p.what64, 8 * per, cudaMemcpyDeviceToHost));
+        return TAGI_OK;
+    }
+    if (which == 3) {
+        std::vector<float> tmp(per);
+        TAGI_CUDA(cudaMemcpy(tmp.data(), p.what32, 4 * per, cudaMemcpyDeviceToHost));
+        for (size_t i = 0; i < per; i++) out[i] = tmp[i];
         return TAGI_OK;
     }
     if ((size_t)numOrbitals > p.scratch_orbitals) return set_error(TAGI_ERR_ARG, "no charges for %d orbitals", numOrbitals);
@@ -451,6 +463,14 @@ int tagi_direct_dev(int numTargets, const double *targetX, const double *targetY
     return direct_sum(numTargets, targetX, targetY, targetZ, targetValue, nsub, subset, numSources, sourceX,
                       sourceY, sourceZ, sourceValue, sourceWeight, output, kernel, kernelParameters[0],
                       singularity, PREC_FP64, (cudaStream_t)stream);
+}
+
+int tagi_pair_peak(int kernel, int singularity, int variant, double kernelParameter, double *pairsPerSecond,
+                   void *stream) {
+    if (!pairsPerSecond) return set_error(TAGI_ERR_ARG, "null output");
+    if (kernel != KERNEL_COULOMB && kernel != KERNEL_YUKAWA) return set_error(TAGI_ERR_UNSUPPORTED, "kernel %d", kernel);
+    if (variant != 0 && variant != 1) return set_error(TAGI_ERR_ARG, "variant must be 0 (near) or 1 (far)");
+    return pair_peak(kernel, singularity, variant, kernelParameter, pairsPerSecond, (cudaStream_t)stream);
 }
 
 int tagi_mgs_dev(double *V, double *U, const double *W, int targetWavefunction, int numPoints,

@@ -72,11 +72,11 @@ int direct_sum(int nt, const double *tx, const double *ty, const double *tz, con
     if (ss) ssc = kernel == KERNEL_YUKAWA ? 4.0 * M_PI / (kp * kp) : 2.0 * M_PI / (kp * kp);
     const int grid = (nsub + DT - 1) / DT;
     if (kernel == KERNEL_YUKAWA) {
-        if (ss) direct_f64<KERNEL_YUKAWA, true><<<grid, DT, 0, s>>>(nsub, sub, tx, ty, tz, tv, ns, sx, sy, sz, sv, sw, kp, ssc, out);
-        else direct_f64<KERNEL_YUKAWA, false><<<grid, DT, 0, s>>>(nsub, sub, tx, ty, tz, tv, ns, sx, sy, sz, sv, sw, kp, ssc, out);
+        if (ss) launch(direct_f64<KERNEL_YUKAWA, true>, grid, DT, 0, s, nsub, sub, tx, ty, tz, tv, ns, sx, sy, sz, sv, sw, kp, ssc, out);
+        else launch(direct_f64<KERNEL_YUKAWA, false>, grid, DT, 0, s, nsub, sub, tx, ty, tz, tv, ns, sx, sy, sz, sv, sw, kp, ssc, out);
     } else {
-        if (ss) direct_f64<KERNEL_COULOMB, true><<<grid, DT, 0, s>>>(nsub, sub, tx, ty, tz, tv, ns, sx, sy, sz, sv, sw, kp, ssc, out);
-        else direct_f64<KERNEL_COULOMB, false><<<grid, DT, 0, s>>>(nsub, sub, tx, ty, tz, tv, ns, sx, sy, sz, sv, sw, kp, ssc, out);
+        if (ss) launch(direct_f64<KERNEL_COULOMB, true>, grid, DT, 0, s, nsub, sub, tx, ty, tz, tv, ns, sx, sy, sz, sv, sw, kp, ssc, out);
+        else launch(direct_f64<KERNEL_COULOMB, false>, grid, DT, 0, s, nsub, sub, tx, ty, tz, tv, ns, sx, sy, sz, sv, sw, kp, ssc, out);
     }
     TAGI_LAUNCH_CHECK();
     return TAGI_OK;

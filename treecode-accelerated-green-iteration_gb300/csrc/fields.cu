@@ -10,8 +10,15 @@
 //     FP32 (targets once per batch, sources/proxy points while staging into
 //     shared memory), so pair distances keep FP32 precision relative to the
 //     batch size rather than to the domain size;
+//   * coordinates are also multiplied by a per-orbital scale sc, so that with
+//     r' = sc r the kernels need no multiply for the exp2 argument:
+//       Yukawa       sc = k log2(e):          e^{-k r}/r     = sc 2^{-r'} / r'
+//       Coulomb SS   sc = a sqrt(log2(e)):    e^{-a^2 r^2}   = 2^{-r'^2},  1/r = sc / r'
+//       Coulomb skip sc = 1
+//     and the factor sc multiplies each target's sum once at the end;
 //   * pair terms and per-tile sums in FP32, rsqrt and exp2 on the MUFU pipe;
-//   * tiles (near) and clusters (far) are added with Kahan compensation;
+//   * pair terms are summed in FP32 runs of 64 (near) or one (n+1)^2 slab
+//     (far) and the runs are added with Kahan compensation;
 //   * the singularity-subtraction term f_i * 4pi/k^2 (Yukawa) or
 //     f_i * 2pi/a^2 (Coulomb) is added in FP64 in the epilogue.
 // FP64 mode: identical structure, FP64 everywhere (exp, sqrt, division).
@@ -49,7 +56,7 @@ struct Fields {
     // target side (sorted order)
     const double *tx, *ty, *tz;
     const int *tbegin, *tend;
-    const double *tcenter;
+    const double *tcenter, *tradius;
     const int *batch_node;
     const int *order;
     int nbatch, nt, norb;
@@ -71,14 +78,16 @@ struct Fields {
     // per orbital
     const float *ft32;            // [norb][nt] sorted target values
     const double *ft64;
-    const float *kc32;            // [norb] kernel constant (see kernel_constant)
+    const float *kc32;            // [norb] coordinate scale sc (see coordinate_scale)
     const double *kp64;           // [norb] kernel parameter k or a
     double *out;                  // [norb][nt] sorted order
 };
 
-// Kernel constant for the exp2 argument: Yukawa -k log2(e), Coulomb SS -a^2 log2(e).
-inline float kernel_constant(int kernel, double kp) {
-    return kernel == KERNEL_YUKAWA ? (float)(-kp * LOG2E) : (float)(-kp * kp * LOG2E);
+// Coordinate scale sc of an orbital (see the header comment).
+inline float coordinate_scale(int kernel, int singularity, double kp) {
+    if (kernel == KERNEL_YUKAWA) return (float)(kp * LOG2E);
+    if (singularity == SING_SUBTRACTION) return (float)(kp * std::sqrt(LOG2E));
+    return 1.0f;
 }
 
 __device__ __forceinline__ int next_item(int *queue, int *s_item) {
@@ -88,22 +97,78 @@ __device__ __forceinline__ int next_item(int *queue, int *s_item) {
     return *s_item;
 }
 
-template <int KERN, bool SS>
-__device__ __forceinline__ float pair_near(float dx, float dy, float dz, float q, float w,
-                                           float fi, float kc, float acc) {
-    float r2 = fmaf(dx, dx, fmaf(dy, dy, dz * dz));
+// One pair in scaled coordinates; MASK drops the coincident (r = 0) pair.
+template <int KERN, bool SS, bool MASK>
+__device__ __forceinline__ float pair_scaled(float dx, float dy, float dz, float q, float w, float fi,
+                                             float acc) {
+    const float r2 = fmaf(dx, dx, fmaf(dy, dy, dz * dz));
     float rinv = rsqrt_mufu(r2);
-    rinv = r2 > 0.f ? rinv : 0.f;  // excludes the coincident (self) pair
+    if (MASK) rinv = r2 > 0.f ? rinv : 0.f;
     if (KERN == KERNEL_YUKAWA) {
-        float g = ex2_mufu(kc * (r2 * rinv)) * rinv;
-        float c = SS ? fmaf(-fi, w, q) : q;
-        return fmaf(g, c, acc);
+        const float g = ex2_mufu(-(r2 * rinv)) * rinv;
+        return fmaf(g, SS ? fmaf(-fi, w, q) : q, acc);
+    } else if (SS) {
+        const float e = ex2_mufu(-r2);
+        return fmaf(rinv, fmaf(-fi * e, w, q), acc);
     } else {
-        if (SS) {
-            float e = ex2_mufu(kc * r2);
-            return fmaf(rinv, fmaf(-fi * e, w, q), acc);
-        }
         return fmaf(rinv, q, acc);
+    }
+}
+
+// Compensated (Kahan) addition of an FP32 partial into (sum, cmp).
+__device__ __forceinline__ void kahan_add(float &sum, float &cmp, float part) {
+    const float y = part - cmp;
+    const float t = sum + y;
+    cmp = (t - sum) - y;
+    sum = t;
+}
+
+// One staged tile against NT targets.  Pairs are summed in FP32 in chunks of
+// KCHUNK and each chunk is added to the target's Kahan sum: a long FP32 run
+// loses ~sqrt(n) u of its total, and singularity subtraction multiplies that
+// loss by |f_i int G| / |phi_i| (often 10-100).
+constexpr int KCHUNK = 64;
+template <int KERN, bool SS, bool MASK, int NT>
+__device__ __forceinline__ void near_tile(const float4 *__restrict__ s_src, const float *__restrict__ s_w,
+                                          int cnt, const float (&tx)[NT], const float (&ty)[NT],
+                                          const float (&tz)[NT], const float (&fi)[NT], float (&sum)[NT],
+                                          float (&cmp)[NT]) {
+    if (cnt == NTILE) {
+#pragma unroll 1
+        for (int j0 = 0; j0 < NTILE; j0 += KCHUNK) {
+            float part[NT];
+#pragma unroll
+            for (int k = 0; k < NT; k++) part[k] = 0.f;
+#pragma unroll 8
+            for (int j = j0; j < j0 + KCHUNK; j++) {
+                const float4 sj = s_src[j];
+                const float w = s_w[j];
+#pragma unroll
+                for (int k = 0; k < NT; k++)
+                    part[k] = pair_scaled<KERN, SS, MASK>(tx[k] - sj.x, ty[k] - sj.y, tz[k] - sj.z, sj.w, w,
+                                                          fi[k], part[k]);
+            }
+#pragma unroll
+            for (int k = 0; k < NT; k++) kahan_add(sum[k], cmp[k], part[k]);
+        }
+    } else {
+        for (int j0 = 0; j0 < cnt; j0 += KCHUNK) {
+            const int j1 = min(j0 + KCHUNK, cnt);
+            float part[NT];
+#pragma unroll
+            for (int k = 0; k < NT; k++) part[k] = 0.f;
+#pragma unroll 4
+            for (int j = j0; j < j1; j++) {
+                const float4 sj = s_src[j];
+                const float w = s_w[j];
+#pragma unroll
+                for (int k = 0; k < NT; k++)
+                    part[k] = pair_scaled<KERN, SS, MASK>(tx[k] - sj.x, ty[k] - sj.y, tz[k] - sj.z, sj.w, w,
+                                                          fi[k], part[k]);
+            }
+#pragma unroll
+            for (int k = 0; k < NT; k++) kahan_add(sum[k], cmp[k], part[k]);
+        }
     }
 }
 
@@ -111,7 +176,7 @@ __device__ __forceinline__ float pair_near(float dx, float dy, float dz, float q
 // Near field, mixed precision.
 // ---------------------------------------------------------------------------
 template <int KERN, bool SS, int NT>
-__global__ void __launch_bounds__(FT) near_mixed(Fields a) {
+__global__ void __launch_bounds__(FT, 3) near_mixed(Fields a) {
     __shared__ float4 s_src[NTILE];
     __shared__ float s_w[NTILE];
     __shared__ int s_item;
@@ -126,75 +191,128 @@ __global__ void __launch_bounds__(FT) near_mixed(Fields a) {
         const int tb = a.tbegin[bn], te = a.tend[bn];
         const double cbx = a.tcenter[3L * bn], cby = a.tcenter[3L * bn + 1],
                      cbz = a.tcenter[3L * bn + 2];
-        const float kc = a.kc32[orb];
+        const float scf = a.kc32[orb];
+        const double sc = (double)scf;
         const float *q = a.q32 + (long)orb * a.ns;
         const float *ft = a.ft32 + (long)orb * a.nt;
         const int r0 = a.rng_off[b], r1 = a.rng_off[b + 1];
         for (int base = tb; base < te; base += FT * NT) {
+            // consecutive targets per thread: the threads with targets form a
+            // prefix, so whole warps past it have none and skip the pair loops
+            const bool warp_busy = base + NT * (tid & ~31) < te;
             float tx[NT], ty[NT], tz[NT], fi[NT], sum[NT], cmp[NT];
 #pragma unroll
             for (int k = 0; k < NT; k++) {
-                int i = base + tid + k * FT;
+                int i = base + NT * tid + k;
                 bool v = i < te;
-                tx[k] = v ? (float)(a.tx[i] - cbx) : 0.f;
-                ty[k] = v ? (float)(a.ty[i] - cby) : 0.f;
-                tz[k] = v ? (float)(a.tz[i] - cbz) : 0.f;
+                tx[k] = v ? (float)(a.tx[i] - cbx) * scf : 0.f;
+                ty[k] = v ? (float)(a.ty[i] - cby) * scf : 0.f;
+                tz[k] = v ? (float)(a.tz[i] - cbz) * scf : 0.f;
                 fi[k] = v ? ft[i] : 0.f;
                 sum[k] = 0.f;
                 cmp[k] = 0.f;
             }
             for (int e = r0; e < r1; e++) {
                 const int2 r = a.rng[e];
-                for (int t0 = r.x; t0 < r.y; t0 += NTILE) {
+                const bool mask = range_may_coincide(r);
+                const int rb = range_begin(r);
+                for (int t0 = rb; t0 < r.y; t0 += NTILE) {
                     const int cnt = min(NTILE, r.y - t0);
                     __syncthreads();
                     for (int j = tid; j < cnt; j += FT) {
                         int jj = t0 + j;
-                        s_src[j] = make_float4((float)(a.sx[jj] - cbx), (float)(a.sy[jj] - cby),
-                                               (float)(a.sz[jj] - cbz), q[jj]);
+                        s_src[j] = make_float4((float)(a.sx[jj] - cbx) * scf, (float)(a.sy[jj] - cby) * scf,
+                                               (float)(a.sz[jj] - cbz) * scf, q[jj]);
                         s_w[j] = a.w32[jj];
                     }
                     __syncthreads();
-                    float part[NT];
-#pragma unroll
-                    for (int k = 0; k < NT; k++) part[k] = 0.f;
-#pragma unroll 4
-                    for (int j = 0; j < cnt; j++) {
-                        const float4 s = s_src[j];
-                        const float w = s_w[j];
-#pragma unroll
-                        for (int k = 0; k < NT; k++)
-                            part[k] = pair_near<KERN, SS>(tx[k] - s.x, ty[k] - s.y, tz[k] - s.z,
-                                                          s.w, w, fi[k], kc, part[k]);
-                    }
-#pragma unroll
-                    for (int k = 0; k < NT; k++) {  // Kahan across tiles
-                        float y = part[k] - cmp[k];
-                        float t = sum[k] + y;
-                        cmp[k] = (t - sum[k]) - y;
-                        sum[k] = t;
-                    }
+                    if (!warp_busy) continue;
+                    if (mask) near_tile<KERN, SS, true, NT>(s_src, s_w, cnt, tx, ty, tz, fi, sum, cmp);
+                    else near_tile<KERN, SS, false, NT>(s_src, s_w, cnt, tx, ty, tz, fi, sum, cmp);
                 }
             }
 #pragma unroll
             for (int k = 0; k < NT; k++) {
-                int i = base + tid + k * FT;
-                if (i < te) a.out[(long)orb * a.nt + i] = (double)sum[k] - (double)cmp[k];
+                int i = base + NT * tid + k;
+                if (i < te) a.out[(long)orb * a.nt + i] = ((double)sum[k] - (double)cmp[k]) * sc;
             }
         }
     }
 }
 
 // ---------------------------------------------------------------------------
-// Far field, mixed precision.  Proxy grid is a tensor product, so r^2 is
-// assembled from per-axis squares: (k1,k2) parts once per 8 pairs.
+// Far field, mixed precision.  The proxy grid is a tensor product, so r'^2
+// is assembled from per-axis squares (one add per pair).  Two targets per
+// thread share every shared-memory read.  Coulomb subtraction: when the
+// whole cluster lies so far that r'^2 > 40 for every proxy point, the
+// Gaussian term f_i what_k 2^{-r'^2} is below 2^-40 of f_i what_k and is
+// dropped (one MUFU op less per pair); Yukawa clusters with r' > 127
+// everywhere add exactly 0 in FP32 (2^{-r'} flushes to zero) and are skipped.
 // ---------------------------------------------------------------------------
-template <int KERN, bool SS, int MAXN1>
-__global__ void __launch_bounds__(FT) far_mixed(Fields a) {
+template <int KERN, bool SS, bool EXPTERM, int MAXN1, int NT>
+__device__ __forceinline__ void far_cluster(const float2 *__restrict__ s_qw, const float (*s_p)[MAXN1],
+                                            int n1, const float (&tx)[NT], const float (&ty)[NT],
+                                            const float (&tz)[NT], const float (&fi)[NT],
+                                            float (&sum)[NT], float (&cmp)[NT]) {
+    float dz2[NT][MAXN1];
+#pragma unroll
+    for (int k = 0; k < NT; k++)
+#pragma unroll
+        for (int m = 0; m < MAXN1; m++) {
+            float d = tz[k] - s_p[2][m < n1 ? m : 0];
+            dz2[k][m] = d * d;
+        }
+    int idx = 0;
+    for (int k1 = 0; k1 < n1; k1++) {  // one (n+1)^2 slab per FP32 partial, then Kahan
+        float part[NT];
+#pragma unroll
+        for (int k = 0; k < NT; k++) part[k] = 0.f;
+        float dx2[NT];
+#pragma unroll
+        for (int k = 0; k < NT; k++) {
+            const float dx = tx[k] - s_p[0][k1];
+            dx2[k] = dx * dx;
+        }
+        for (int k2 = 0; k2 < n1; k2++) {
+            float rxy[NT];
+#pragma unroll
+            for (int k = 0; k < NT; k++) {
+                const float dy = ty[k] - s_p[1][k2];
+                rxy[k] = fmaf(dy, dy, dx2[k]);
+            }
+#pragma unroll
+            for (int k3 = 0; k3 < MAXN1; k3++) {
+                if (k3 < n1) {
+                    const float2 qw = s_qw[idx + k3];
+#pragma unroll
+                    for (int k = 0; k < NT; k++) {
+                        const float r2 = rxy[k] + dz2[k][k3];
+                        const float rinv = rsqrt_mufu(r2);
+                        if (KERN == KERNEL_YUKAWA) {
+                            const float g = ex2_mufu(-(r2 * rinv)) * rinv;
+                            part[k] = fmaf(g, SS ? fmaf(-fi[k], qw.y, qw.x) : qw.x, part[k]);
+                        } else if (SS && EXPTERM) {
+                            const float ex = ex2_mufu(-r2);
+                            part[k] = fmaf(rinv, fmaf(-fi[k] * ex, qw.y, qw.x), part[k]);
+                        } else {
+                            part[k] = fmaf(rinv, qw.x, part[k]);
+                        }
+                    }
+                }
+            }
+            idx += n1;
+        }
+#pragma unroll
+        for (int k = 0; k < NT; k++) kahan_add(sum[k], cmp[k], part[k]);
+    }
+}
+
+template <int KERN, bool SS, int MAXN1, int NT>
+__global__ void __launch_bounds__(FT, 2) far_mixed(Fields a) {
     constexpr int MAXP = MAXN1 * MAXN1 * MAXN1;
     __shared__ float2 s_qw[MAXP];
     __shared__ float s_p[3][MAXN1];
-    __shared__ int s_item;
+    __shared__ int s_item, s_mode;
     const int tid = threadIdx.x;
     const int n1 = a.n1, P = a.P;
     const int total = a.nbatch * a.norb;
@@ -208,69 +326,59 @@ __global__ void __launch_bounds__(FT) far_mixed(Fields a) {
         const int bn = a.batch_node[b];
         const int tb = a.tbegin[bn], te = a.tend[bn];
         const double cb[3] = {a.tcenter[3L * bn], a.tcenter[3L * bn + 1], a.tcenter[3L * bn + 2]};
-        const float kc = a.kc32[orb];
+        const double rb = a.tradius[bn];
+        const float scf = a.kc32[orb];
+        const double sc = (double)scf;
         const float *ft = a.ft32 + (long)orb * a.nt;
         const float *qh = a.qhat32 + (long)orb * a.nslots * P;
-        for (int base = tb; base < te; base += FT) {
-            const int i = base + tid;
-            const bool v = i < te;
-            const float tx = v ? (float)(a.tx[i] - cb[0]) : 0.f;
-            const float ty = v ? (float)(a.ty[i] - cb[1]) : 0.f;
-            const float tz = v ? (float)(a.tz[i] - cb[2]) : 0.f;
-            const float fi = v ? ft[i] : 0.f;
-            float sum = 0.f, cmp = 0.f;
+        for (int base = tb; base < te; base += FT * NT) {
+            const bool warp_busy = base + NT * (tid & ~31) < te;
+            float tx[NT], ty[NT], tz[NT], fi[NT], sum[NT], cmp[NT];
+#pragma unroll
+            for (int k = 0; k < NT; k++) {
+                const int i = base + NT * tid + k;
+                const bool v = i < te;
+                tx[k] = v ? (float)(a.tx[i] - cb[0]) * scf : 0.f;
+                ty[k] = v ? (float)(a.ty[i] - cb[1]) * scf : 0.f;
+                tz[k] = v ? (float)(a.tz[i] - cb[2]) * scf : 0.f;
+                fi[k] = v ? ft[i] : 0.f;
+                sum[k] = 0.f;
+                cmp[k] = 0.f;
+            }
             for (int e = f0; e < f1; e++) {
                 const int slot = a.node_slot[a.far_list[e]];
+                const double *g = a.geom + 6L * slot;
                 __syncthreads();
                 const float *qs = qh + (long)slot * P;
                 const float *ws = a.what32 + (long)slot * P;
                 for (int k = tid; k < P; k += FT) s_qw[k] = make_float2(qs[k], ws[k]);
                 if (tid < 3 * n1) {
-                    int d = tid / n1, m = tid - d * n1;
-                    const double *g = a.geom + 6L * slot;
-                    s_p[d][m] = (float)((g[d] + g[3 + d] * a.tn[m]) - cb[d]);
+                    const int d = tid / n1, m = tid - d * n1;
+                    const double cbd = d == 0 ? cb[0] : (d == 1 ? cb[1] : cb[2]);
+                    s_p[d][m] = (float)((g[d] + g[3 + d] * a.tn[m]) - cbd) * scf;
+                }
+                if (tid == 0) {
+                    // smallest scaled distance from the batch to the proxy box (conservative)
+                    const double dx = cb[0] - g[0], dy = cb[1] - g[1], dz = cb[2] - g[2];
+                    const double rc = sqrt(g[3] * g[3] + g[4] * g[4] + g[5] * g[5]);
+                    const double dmin = (sqrt(dx * dx + dy * dy + dz * dz) - rb - rc) * sc * (1.0 - 1e-6);
+                    int mode = 0;
+                    if (KERN == KERNEL_YUKAWA && dmin > 127.0) mode = 2;  // 2^{-r'} flushes to 0: adds exactly 0
+                    // Gaussian correction below 2^-40 of its own term everywhere: dropped
+                    if (KERN == KERNEL_COULOMB && SS && dmin > 0.0 && dmin * dmin > 40.0) mode = 1;
+                    s_mode = mode;
                 }
                 __syncthreads();
-                float dz2[MAXN1];
-#pragma unroll
-                for (int m = 0; m < MAXN1; m++) {
-                    float d = tz - s_p[2][m < n1 ? m : 0];
-                    dz2[m] = d * d;
-                }
-                float part = 0.f;
-                int idx = 0;
-                for (int k1 = 0; k1 < n1; k1++) {
-                    const float dx = tx - s_p[0][k1];
-                    const float dx2 = dx * dx;
-                    for (int k2 = 0; k2 < n1; k2++) {
-                        const float dy = ty - s_p[1][k2];
-                        const float rxy = fmaf(dy, dy, dx2);
-#pragma unroll
-                        for (int k3 = 0; k3 < MAXN1; k3++) {
-                            if (k3 < n1) {
-                                const float r2 = rxy + dz2[k3];
-                                const float rinv = rsqrt_mufu(r2);
-                                const float2 qw = s_qw[idx + k3];
-                                if (KERN == KERNEL_YUKAWA) {
-                                    const float g = ex2_mufu(kc * (r2 * rinv)) * rinv;
-                                    part = fmaf(g, SS ? fmaf(-fi, qw.y, qw.x) : qw.x, part);
-                                } else if (SS) {
-                                    const float ex = ex2_mufu(kc * r2);
-                                    part = fmaf(rinv, fmaf(-fi * ex, qw.y, qw.x), part);
-                                } else {
-                                    part = fmaf(rinv, qw.x, part);
-                                }
-                            }
-                        }
-                        idx += n1;
-                    }
-                }
-                float y = part - cmp;
-                float t = sum + y;
-                cmp = (t - sum) - y;
-                sum = t;
+                const int mode = s_mode;
+                if (mode == 2 || !warp_busy) continue;
+                if (mode == 1) far_cluster<KERN, SS, false, MAXN1, NT>(s_qw, s_p, n1, tx, ty, tz, fi, sum, cmp);
+                else far_cluster<KERN, SS, true, MAXN1, NT>(s_qw, s_p, n1, tx, ty, tz, fi, sum, cmp);
             }
-            if (v) a.out[(long)orb * a.nt + i] = (double)sum - (double)cmp;
+#pragma unroll
+            for (int k = 0; k < NT; k++) {
+                const int i = base + NT * tid + k;
+                if (i < te) a.out[(long)orb * a.nt + i] = ((double)sum[k] - (double)cmp[k]) * sc;
+            }
         }
     }
 }
@@ -319,7 +427,7 @@ __global__ void __launch_bounds__(FT) near_f64(Fields a) {
             double acc = 0.0;
             for (int e = r0; e < r1; e++) {
                 const int2 r = a.rng[e];
-                for (int t0 = r.x; t0 < r.y; t0 += T64) {
+                for (int t0 = range_begin(r); t0 < r.y; t0 += T64) {
                     const int cnt = min(T64, r.y - t0);
                     __syncthreads();
                     if (tid < cnt) {
@@ -436,15 +544,19 @@ __global__ void prep_targets(const double *__restrict__ tv, const int *__restric
     f64[(long)orb * nt + i] = f;
 }
 
+// phi_i = near + far + f_i * SS factor, scattered back to caller order.  The
+// SS term uses the same f_i the pair sums used (FP32-rounded in mixed mode):
+// sum_j w_j (f_j - c) G + c * int G is exact for any constant c, while mixing
+// two roundings of f_i would leave delta * f_i * sum_j w_j G in the result.
+template <typename TF>
 __global__ void epilogue(const double *__restrict__ nearv, const double *__restrict__ farv,
-                         const double *__restrict__ tv, const int *__restrict__ perm, int nt,
+                         const TF *__restrict__ fsorted, const int *__restrict__ perm, int nt,
                          const double *__restrict__ ss, double *__restrict__ out) {
     long i = (long)blockIdx.x * blockDim.x + threadIdx.x;
     int orb = blockIdx.y;
     if (i >= nt) return;
-    long o = (long)orb * nt + perm[i];
     long si = (long)orb * nt + i;
-    out[o] = nearv[si] + farv[si] + ss[orb] * tv[o];
+    out[(long)orb * nt + perm[i]] = nearv[si] + farv[si] + ss[orb] * (double)fsorted[si];
 }
 
 template <typename K>
@@ -463,8 +575,89 @@ int launch_persistent(K kern, const Fields &a, int items, cudaStream_t s) {
     TAGI_TRY(occupancy_grid(kern, &grid));
     if (grid > items) grid = items;
     if (grid < 1) grid = 1;
-    kern<<<grid, FT, 0, s>>>(a);
+    launch(kern, grid, FT, 0, s, a);
     TAGI_LAUNCH_CHECK();
+    return TAGI_OK;
+}
+
+// ---------------------------------------------------------------------------
+// Pair-throughput ceiling: the near/far inner loops' arithmetic with operands
+// already in shared memory and registers and no global traffic.  The field
+// kernels' roofline fraction is measured against this, live, on the same GPU.
+// ---------------------------------------------------------------------------
+template <int KERN, bool SS>
+__global__ void __launch_bounds__(FT) pair_peak_near(int reps, float *out) {
+    __shared__ float4 s_src[NTILE];
+    __shared__ float s_w[NTILE];
+    for (int j = threadIdx.x; j < NTILE; j += FT) {
+        float v = (float)((j * 37) % 101) * 0.01f - 0.5f;
+        s_src[j] = make_float4(v, 0.3f * v + 0.1f, 0.7f - v, 0.5f + 0.001f * j);
+        s_w[j] = 0.25f;
+    }
+    __syncthreads();
+    float tx[2], ty[2], tz[2], fi[2], sum[2] = {0.f, 0.f}, cmp[2] = {0.f, 0.f};
+    for (int k = 0; k < 2; k++) {
+        tx[k] = 0.01f * (threadIdx.x & 31) + 0.003f * k;
+        ty[k] = 0.02f;
+        tz[k] = -0.03f * (threadIdx.x >> 5);
+        fi[k] = 0.3f;
+    }
+    for (int r = 0; r < reps; r++) near_tile<KERN, SS, false, 2>(s_src, s_w, NTILE, tx, ty, tz, fi, sum, cmp);
+    out[blockIdx.x * FT + threadIdx.x] = sum[0] + sum[1] - cmp[0] - cmp[1];
+}
+
+template <int KERN, bool SS>
+__global__ void __launch_bounds__(FT) pair_peak_far(int reps, float *out) {
+    constexpr int N1 = 8;
+    __shared__ float2 s_qw[N1 * N1 * N1];
+    __shared__ float s_p[3][N1];
+    for (int k = threadIdx.x; k < N1 * N1 * N1; k += FT) s_qw[k] = make_float2(0.5f + 0.001f * k, 0.25f);
+    if (threadIdx.x < 3 * N1) s_p[threadIdx.x / N1][threadIdx.x % N1] = 1.0f + 0.1f * threadIdx.x;
+    __syncthreads();
+    float tx[2], ty[2], tz[2], fi[2], sum[2] = {0.f, 0.f}, cmp[2] = {0.f, 0.f};
+    for (int k = 0; k < 2; k++) {
+        tx[k] = 0.01f * (threadIdx.x & 31) + 0.003f * k;
+        ty[k] = 0.02f;
+        tz[k] = -0.03f * (threadIdx.x >> 5);
+        fi[k] = 0.3f;
+    }
+    for (int r = 0; r < reps; r++) far_cluster<KERN, SS, true, N1, 2>(s_qw, s_p, N1, tx, ty, tz, fi, sum, cmp);
+    out[blockIdx.x * FT + threadIdx.x] = sum[0] + sum[1] - cmp[0] - cmp[1];
+}
+
+template <int KERN, bool SS>
+int run_pair_peak(int variant, double *pairs_per_s, cudaStream_t s) {
+    int grid = 0;
+    if (variant == 0) TAGI_TRY(occupancy_grid(pair_peak_near<KERN, SS>, &grid));
+    else TAGI_TRY(occupancy_grid(pair_peak_far<KERN, SS>, &grid));
+    Arena tmp;
+    tmp.stream = s;
+    float *out = nullptr;
+    TAGI_TRY(tmp.alloc(&out, (size_t)grid * FT));
+    cudaEvent_t a, b;
+    cudaEventCreate(&a);
+    cudaEventCreate(&b);
+    const int per_rep = 2 * (variant == 0 ? NTILE : 512);  // two targets per thread
+    int reps = 16;
+    float ms = 0.f;
+    int rc = TAGI_OK;
+    for (int attempt = 0; attempt < 6; attempt++) {  // grow until the timed launch lasts >= 20 ms
+        if (variant == 0) launch(pair_peak_near<KERN, SS>, grid, FT, 0, s, reps, out);
+        else launch(pair_peak_far<KERN, SS>, grid, FT, 0, s, reps, out);
+        cudaEventRecord(a, s);
+        if (variant == 0) launch(pair_peak_near<KERN, SS>, grid, FT, 0, s, reps, out);
+        else launch(pair_peak_far<KERN, SS>, grid, FT, 0, s, reps, out);
+        cudaEventRecord(b, s);
+        if (cudaEventSynchronize(b) != cudaSuccess) { rc = set_error(TAGI_ERR_CUDA, "pair peak launch failed"); break; }
+        cudaEventElapsedTime(&ms, a, b);
+        if (ms >= 20.f) break;
+        reps *= 4;
+    }
+    cudaEventDestroy(a);
+    cudaEventDestroy(b);
+    tmp.release();
+    if (rc) return rc;
+    *pairs_per_s = (double)grid * FT * per_rep * reps / (ms * 1e-3);
     return TAGI_OK;
 }
 
@@ -476,20 +669,33 @@ int launch_fields(Plan &p, const Fields &a, int precision, cudaStream_t s) {
     an.out = p.near_out;
     af.order = p.order_far;
     af.out = p.far_out;
+    phase_mark(PH_NEAR, true, s);
+    const bool one = p.max_batch <= FT;  // one target per thread covers every batch
     if (precision == PREC_MIXED) {
-        if (p.max_batch <= FT) TAGI_TRY(launch_persistent(near_mixed<KERN, SS, 1>, an, items, s));
+        if (one) TAGI_TRY(launch_persistent(near_mixed<KERN, SS, 1>, an, items, s));
         else TAGI_TRY(launch_persistent(near_mixed<KERN, SS, 2>, an, items, s));
-        if (p.nslots == 0) return TAGI_OK;
-        if (p.n1 <= 4) TAGI_TRY(launch_persistent(far_mixed<KERN, SS, 4>, af, items, s));
-        else if (p.n1 <= 8) TAGI_TRY(launch_persistent(far_mixed<KERN, SS, 8>, af, items, s));
-        else TAGI_TRY(launch_persistent(far_mixed<KERN, SS, MAX_DEGREE + 1>, af, items, s));
     } else {
         TAGI_TRY(launch_persistent(near_f64<KERN, SS>, an, items, s));
-        if (p.nslots == 0) return TAGI_OK;
+    }
+    phase_mark(PH_NEAR, false, s);
+    if (p.nslots == 0) return TAGI_OK;
+    phase_mark(PH_FAR, true, s);
+    if (precision == PREC_MIXED) {
+        if (one) {
+            if (p.n1 <= 4) TAGI_TRY(launch_persistent(far_mixed<KERN, SS, 4, 1>, af, items, s));
+            else if (p.n1 <= 8) TAGI_TRY(launch_persistent(far_mixed<KERN, SS, 8, 1>, af, items, s));
+            else TAGI_TRY(launch_persistent(far_mixed<KERN, SS, MAX_DEGREE + 1, 1>, af, items, s));
+        } else {
+            if (p.n1 <= 4) TAGI_TRY(launch_persistent(far_mixed<KERN, SS, 4, 2>, af, items, s));
+            else if (p.n1 <= 8) TAGI_TRY(launch_persistent(far_mixed<KERN, SS, 8, 2>, af, items, s));
+            else TAGI_TRY(launch_persistent(far_mixed<KERN, SS, MAX_DEGREE + 1, 2>, af, items, s));
+        }
+    } else {
         if (p.n1 <= 4) TAGI_TRY(launch_persistent(far_f64<KERN, SS, 4>, af, items, s));
         else if (p.n1 <= 8) TAGI_TRY(launch_persistent(far_f64<KERN, SS, 8>, af, items, s));
         else TAGI_TRY(launch_persistent(far_f64<KERN, SS, MAX_DEGREE + 1>, af, items, s));
     }
+    phase_mark(PH_FAR, false, s);
     return TAGI_OK;
 }
 
@@ -534,7 +740,7 @@ int convolve(Plan &p, const double *tv, const double *sv, double *out, int norb,
     for (int o = 0; o < norb; o++) {
         double k = kparams[(long)o * nkp];
         p.h_kp[o] = k;
-        p.h_kc[o] = kernel_constant(kernel, k);
+        p.h_kc[o] = coordinate_scale(kernel, singularity, k);
         p.h_ss[o] = 0.0;
         if (ss) p.h_ss[o] = kernel == KERNEL_YUKAWA ? 4.0 * M_PI / (k * k) : 2.0 * M_PI / (k * k);
     }
@@ -543,10 +749,17 @@ int convolve(Plan &p, const double *tv, const double *sv, double *out, int norb,
     TAGI_CUDA(cudaMemcpyAsync(p.d_ss, p.h_ss.data(), sizeof(double) * norb, cudaMemcpyHostToDevice, s));
 
     dim3 gs((ns + 255) / 256, norb), gt((nt + 255) / 256, norb);
-    prep_sources<<<gs, 256, 0, s>>>(sv, p.src.perm, p.sw64, ns, norb, p.q32, p.q64, p.f64s);
-    prep_targets<<<gt, 256, 0, s>>>(tv, p.tgt.perm, nt, p.ft32, p.ft64);
+    phase_mark(PH_GLUE, true, s);
+    launch(prep_sources, gs, 256, 0, s, sv, p.src.perm, p.sw64, ns, norb, p.q32, p.q64, p.f64s);
+    launch(prep_targets, gt, 256, 0, s, tv, p.tgt.perm, nt, p.ft32, p.ft64);
+    phase_mark(PH_GLUE, false, s);
     TAGI_LAUNCH_CHECK();
+    phase_mark(PH_UPWARD, true, s);
     TAGI_TRY(modified_charges(p, mixed ? PREC_MIXED : PREC_FP64, norb, s));
+    if (!mixed) TAGI_TRY(ensure_weight_charges64(p, s));  // before p.what64 is read below
+    phase_mark(PH_UPWARD, false, s);
+    if (!mixed && p.nslots && !p.what64)
+        return set_error(TAGI_ERR_DEVICE, "FP64 weight charges missing");
 
     Fields a{};
     a.tx = p.tgt.x;
@@ -555,6 +768,7 @@ int convolve(Plan &p, const double *tv, const double *sv, double *out, int norb,
     a.tbegin = p.tgt.begin;
     a.tend = p.tgt.end;
     a.tcenter = p.tgt.center;
+    a.tradius = p.tgt.radius;
     a.batch_node = p.batch_node;
     a.nbatch = p.nbatch;
     a.nt = nt;
@@ -596,9 +810,22 @@ int convolve(Plan &p, const double *tv, const double *sv, double *out, int norb,
         if (ss) TAGI_TRY((launch_fields<KERNEL_COULOMB, true>(p, a, precision, s)));
         else TAGI_TRY((launch_fields<KERNEL_COULOMB, false>(p, a, precision, s)));
     }
-    epilogue<<<gt, 256, 0, s>>>(p.near_out, p.far_out, tv, p.tgt.perm, nt, p.d_ss, out);
+    phase_mark(PH_GLUE, true, s);
+    if (mixed) launch(epilogue<float>, gt, 256, 0, s, p.near_out, p.far_out, p.ft32, p.tgt.perm, nt, p.d_ss, out);
+    else launch(epilogue<double>, gt, 256, 0, s, p.near_out, p.far_out, p.ft64, p.tgt.perm, nt, p.d_ss, out);
+    phase_mark(PH_GLUE, false, s);
     TAGI_LAUNCH_CHECK();
     return TAGI_OK;
+}
+
+int pair_peak(int kernel, int singularity, int variant, double kp, double *pairs_per_s, cudaStream_t s) {
+    (void)kp;
+    const bool ss = singularity == SING_SUBTRACTION;
+    if (kernel == KERNEL_YUKAWA)
+        return ss ? run_pair_peak<KERNEL_YUKAWA, true>(variant, pairs_per_s, s)
+                  : run_pair_peak<KERNEL_YUKAWA, false>(variant, pairs_per_s, s);
+    return ss ? run_pair_peak<KERNEL_COULOMB, true>(variant, pairs_per_s, s)
+              : run_pair_peak<KERNEL_COULOMB, false>(variant, pairs_per_s, s);
 }
 
 }  // namespace tagi

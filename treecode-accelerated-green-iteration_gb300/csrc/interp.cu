@@ -107,7 +107,7 @@ int interp_device(const double *cX, const double *cY, const double *cZ, const do
     (void)h_ppc_c;
     (void)h_ppc_f;
     if (coarseN == fineN) {
-        if (coarseN > 0) copy_all<<<(coarseN + 255) / 256, 256, 0, s>>>(cF, fF, coarseN);
+        if (coarseN > 0) launch(copy_all, (coarseN + 255) / 256, 256, 0, s, cF, fF, coarseN);
         TAGI_LAUNCH_CHECK();
         return TAGI_OK;
     }
@@ -146,7 +146,7 @@ int interp_device(const double *cX, const double *cY, const double *cZ, const do
             rc = set_error(TAGI_ERR_CUDA, "interpolation weight upload failed");
             break;
         }
-        interp_cells<<<ncells, IT, 0, s>>>(cX, cY, cZ, cF, ppc_c, off_c, fX, fY, fZ, fF, ppc_f, off_f,
+        launch(interp_cells, ncells, IT, 0, s, cX, cY, cZ, cF, ppc_c, off_c, fX, fY, fZ, fF, ppc_f, off_f,
                                            p1, d_w, err);
         int h_err = 0;
         if (cudaGetLastError() != cudaSuccess ||

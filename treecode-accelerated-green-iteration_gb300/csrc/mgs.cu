@@ -130,11 +130,11 @@ int mgs_device(double *V, double *U, const double *W, int target, int npts, int 
             break;
         if (target > 0) {
             dim3 g((unsigned)nblk, (unsigned)((target + RB - 1) / RB));
-            mgs_dots<<<g, MT, 0, s>>>(V, U, W, target, npts, chunk, partial);
-            mgs_reduce_rows<<<(target + 127) / 128, 128, 0, s>>>(partial, (int)nblk, target, r);
+            launch(mgs_dots, g, MT, 0, s, V, U, W, target, npts, chunk, partial);
+            launch(mgs_reduce_rows, (target + 127) / 128, 128, 0, s, partial, (int)nblk, target, r);
         }
-        mgs_subtract<<<(unsigned)nblk, MT, 0, s>>>(V, U, W, r, target, npts, chunk, npart);
-        mgs_normalize<<<(unsigned)nblk, MT, 0, s>>>(V, U, npart, (int)nblk, target, npts, chunk);
+        launch(mgs_subtract, (unsigned)nblk, MT, 0, s, V, U, W, r, target, npts, chunk, npart);
+        launch(mgs_normalize, (unsigned)nblk, MT, 0, s, V, U, npart, (int)nblk, target, npts, chunk);
         if (cudaGetLastError() != cudaSuccess) rc = set_error(TAGI_ERR_CUDA, "MGS kernels failed");
     } while (0);
     tmp.release();

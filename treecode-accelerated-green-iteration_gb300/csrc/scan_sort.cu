@@ -78,17 +78,17 @@ int exclusive_scan(const int *in, int *out, int n, int *d_total, Arena &ar, cuda
     int nb = (n + SCAN_TILE - 1) / SCAN_TILE;
     int *sums = nullptr;
     TAGI_TRY(ar.alloc(&sums, nb + 1));
-    scan_tiles<<<nb, SCAN_THREADS, 0, s>>>(in, out, n, sums);
+    launch(scan_tiles, nb, SCAN_THREADS, 0, s, in, out, n, sums);
     TAGI_LAUNCH_CHECK();
     if (nb == 1) {
-        if (d_total) copy_one<<<1, 1, 0, s>>>(sums, d_total);
+        if (d_total) launch(copy_one, 1, 1, 0, s, sums, d_total);
         TAGI_LAUNCH_CHECK();
         return TAGI_OK;
     }
     int *offs = nullptr;
     TAGI_TRY(ar.alloc(&offs, nb));
     TAGI_TRY(exclusive_scan(sums, offs, nb, d_total, ar, s));
-    add_tile_offsets<<<nb, 256, 0, s>>>(out, n, offs);
+    launch(add_tile_offsets, nb, 256, 0, s, out, n, offs);
     TAGI_LAUNCH_CHECK();
     return TAGI_OK;
 }
@@ -178,10 +178,10 @@ int radix_sort_u64(uint64_t *keys, int *vals, int n, Arena &ar, cudaStream_t s) 
     uint64_t *ka = keys, *kb = k2;
     int *va = vals, *vb = v2;
     for (int shift = 0; shift < 64; shift += 8) {
-        rs_histogram<<<nb, RS_THREADS, 0, s>>>(ka, n, shift, hist, nb);
+        launch(rs_histogram, nb, RS_THREADS, 0, s, ka, n, shift, hist, nb);
         TAGI_LAUNCH_CHECK();
         TAGI_TRY(exclusive_scan(hist, offs, 256 * nb, nullptr, ar, s));
-        rs_scatter<<<nb, RS_THREADS, 0, s>>>(ka, va, kb, vb, n, shift, offs, nb);
+        launch(rs_scatter, nb, RS_THREADS, 0, s, ka, va, kb, vb, n, shift, offs, nb);
         TAGI_LAUNCH_CHECK();
         uint64_t *kt = ka; ka = kb; kb = kt;
         int *vt = va; va = vb; vb = vt;

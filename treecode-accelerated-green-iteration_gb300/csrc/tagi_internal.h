@@ -14,6 +14,7 @@
 #include <cuda_runtime.h>
 #include <cstdint>
 #include <cstdio>
+#include <utility>
 #include <vector>
 
 #include "../../include/tagi_gb300.h"  // status codes TAGI_OK, TAGI_ERR_*
@@ -49,6 +50,27 @@ int last_error();
     } while (0)
 
 #define TAGI_LAUNCH_CHECK() TAGI_CUDA(cudaGetLastError())
+
+// Every kernel of the library goes through launch(): it counts launches
+// (tagi_launch_count) so a caller can state how many kernels ran.
+void count_launch();
+template <typename... KArgs, typename... Args>
+inline void launch(void (*kern)(KArgs...), dim3 grid, dim3 block, size_t smem, cudaStream_t s,
+                   Args &&...args) {
+    count_launch();
+    kern<<<grid, block, smem, s>>>(std::forward<Args>(args)...);
+}
+
+// Merged near ranges are int2 {begin, end} in sorted source order; bit 31 of
+// begin marks a range whose box touches the batch's box, where a source may
+// coincide with a target.  Always decode through these two helpers.
+__host__ __device__ __forceinline__ int range_begin(int2 r) { return r.x & 0x7fffffff; }
+__host__ __device__ __forceinline__ bool range_may_coincide(int2 r) { return r.x < 0; }
+
+// Optional per-phase timing with CUDA events on the launching stream
+// (tagi_profile / tagi_profile_read); no-ops unless enabled.
+enum Phase { PH_TREE = 0, PH_LISTS, PH_UPWARD, PH_NEAR, PH_FAR, PH_GLUE, PH_COUNT };
+void phase_mark(int phase, bool begin, cudaStream_t s);
 
 // Stream-ordered device allocations owned by a plan (freed on destroy).
 struct Arena {
@@ -111,7 +133,8 @@ struct Plan {
     double *sw64 = nullptr;                // sorted source weights
     float *sw32 = nullptr;
     float *what32 = nullptr;               // weight modified charges [slot][P]
-    double *what64 = nullptr;
+    double *what64 = nullptr;              // FP64 set, built on first FP64 use
+    bool what64_ready = false;
     int *order_near = nullptr, *order_far = nullptr;   // batches, heaviest first
     int *queue = nullptr;                  // work-queue counters (2 ints)
     int *err_flag = nullptr;
@@ -147,6 +170,7 @@ int build_lists(Plan &p, cudaStream_t s);
 
 // upward.cu
 int build_weight_charges(Plan &p, cudaStream_t s);
+int ensure_weight_charges64(Plan &p, cudaStream_t s);
 int modified_charges(Plan &p, int precision, int norb, cudaStream_t s);
 
 // fields.cu
@@ -157,6 +181,8 @@ int direct_sum(int nt, const double *tx, const double *ty, const double *tz, con
                int nsub, const int *sub, int ns, const double *sx, const double *sy,
                const double *sz, const double *sv, const double *sw, double *out, int kernel,
                double kp, int singularity, int precision, cudaStream_t s);
+
+int pair_peak(int kernel, int singularity, int variant, double kp, double *pairs_per_s, cudaStream_t s);
 
 // mgs.cu / interp.cu
 int mgs_device(double *V, double *U, const double *W, int target, int npts, int nwave,

@@ -65,14 +65,36 @@ __global__ void bbox_partial(const double *__restrict__ x, const double *__restr
     }
 }
 
-// params[0..2] = lower corner, params[3] = 2^21 / cube edge.
-__global__ void bbox_final(const double *__restrict__ part, int nb, double *__restrict__ params) {
-    if (threadIdx.x != 0) return;
+// params[0..2] = lower corner, params[3] = 2^21 / cube edge.  One block
+// reduces the per-block partials (min/max are exact in any order).
+__global__ void __launch_bounds__(256) bbox_final(const double *__restrict__ part, int nb,
+                                                  double *__restrict__ params) {
     double l[3] = {part[0], part[1], part[2]}, h[3] = {part[3], part[4], part[5]};
-    for (int b = 1; b < nb; b++)
+    for (int b = threadIdx.x; b < nb; b += blockDim.x)
         for (int d = 0; d < 3; d++) {
             l[d] = dmin(l[d], part[b * 6 + d]);
             h[d] = dmax(h[d], part[b * 6 + 3 + d]);
+        }
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1)
+#pragma unroll
+        for (int d = 0; d < 3; d++) {
+            l[d] = dmin(l[d], __shfl_xor_sync(0xffffffffu, l[d], o));
+            h[d] = dmax(h[d], __shfl_xor_sync(0xffffffffu, h[d], o));
+        }
+    __shared__ double sl[8][6];
+    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+    if (lane == 0)
+        for (int d = 0; d < 3; d++) {
+            sl[wid][d] = l[d];
+            sl[wid][3 + d] = h[d];
+        }
+    __syncthreads();
+    if (threadIdx.x != 0) return;
+    for (int w = 1; w < (int)(blockDim.x >> 5); w++)
+        for (int d = 0; d < 3; d++) {
+            l[d] = dmin(l[d], sl[w][d]);
+            h[d] = dmax(h[d], sl[w][3 + d]);
         }
     double ext = __dsub_rn(h[0], l[0]);
     if (__dsub_rn(h[1], l[1]) > ext) ext = __dsub_rn(h[1], l[1]);
@@ -262,15 +284,15 @@ int build_tree(Tree &t, const double *x, const double *y, const double *z, int n
         double *part = nullptr, *params = nullptr;
         if ((rc = tmp.alloc(&part, 6L * nbb))) break;
         if ((rc = tmp.alloc(&params, 4))) break;
-        bbox_partial<<<nbb, 256, 0, s>>>(x, y, z, n, part);
-        bbox_final<<<1, 32, 0, s>>>(part, nbb, params);
+        launch(bbox_partial, nbb, 256, 0, s, x, y, z, n, part);
+        launch(bbox_final, 1, 256, 0, s, part, nbb, params);
         if ((rc = ar.alloc(&t.codes, n))) break;
         if ((rc = ar.alloc(&t.perm, n))) break;
-        morton_codes<<<(n + 255) / 256, 256, 0, s>>>(x, y, z, n, params, t.codes, t.perm);
+        launch(morton_codes, (n + 255) / 256, 256, 0, s, x, y, z, n, params, t.codes, t.perm);
         if (cudaGetLastError() != cudaSuccess) { rc = set_error(TAGI_ERR_CUDA, "morton launch"); break; }
         if ((rc = radix_sort_u64(t.codes, t.perm, n, tmp, s))) break;
         if ((rc = ar.alloc(&t.x, n)) || (rc = ar.alloc(&t.y, n)) || (rc = ar.alloc(&t.z, n))) break;
-        gather3<<<(n + 255) / 256, 256, 0, s>>>(x, y, z, t.perm, n, t.x, t.y, t.z);
+        launch(gather3, (n + 255) / 256, 256, 0, s, x, y, z, t.perm, n, t.x, t.y, t.z);
 
         const long cap = 2L * n + 1;
         if ((rc = ar.alloc(&t.begin, cap)) || (rc = ar.alloc(&t.end, cap)) ||
@@ -280,14 +302,14 @@ int build_tree(Tree &t, const double *x, const double *y, const double *z, int n
         int *cc = nullptr, *off = nullptr, *total = nullptr;
         if ((rc = tmp.alloc(&cc, cap)) || (rc = tmp.alloc(&off, cap)) || (rc = tmp.alloc(&total, 1)))
             break;
-        init_root<<<1, 1, 0, s>>>(t.begin, t.end, t.parent, n);
+        launch(init_root, 1, 1, 0, s, t.begin, t.end, t.parent, n);
         t.level_start.assign(1, 0);
         int ls = 0, le = 1;
         while (ls < le) {
             int m = le - ls;
-            count_children<<<(m + 127) / 128, 128, 0, s>>>(t.codes, t.begin, t.end, ls, le, leaf, cc);
+            launch(count_children, (m + 127) / 128, 128, 0, s, t.codes, t.begin, t.end, ls, le, leaf, cc);
             if ((rc = exclusive_scan(cc, off, m, total, tmp, s))) break;
-            fill_children<<<(m + 127) / 128, 128, 0, s>>>(t.codes, t.begin, t.end, t.parent,
+            launch(fill_children, (m + 127) / 128, 128, 0, s, t.codes, t.begin, t.end, t.parent,
                                                           t.first_child, t.nchild, ls, le, cc, off);
             int h_total = 0;
             if (cudaMemcpyAsync(&h_total, total, sizeof(int), cudaMemcpyDeviceToHost, s) !=
@@ -313,7 +335,7 @@ int build_tree(Tree &t, const double *x, const double *y, const double *z, int n
         for (int lv = t.nlevels - 1; lv >= 0; lv--) {
             int a = t.level_start[lv], b = t.level_start[lv + 1];
             int warps = b - a;
-            node_boxes<<<(warps * 32 + 255) / 256, 256, 0, s>>>(a, b, t.begin, t.end, t.first_child,
+            launch(node_boxes, (warps * 32 + 255) / 256, 256, 0, s, a, b, t.begin, t.end, t.first_child,
                                                                 t.nchild, t.x, t.y, t.z, box,
                                                                 t.center, t.half, t.radius);
         }
@@ -424,33 +446,69 @@ __global__ void assign_slots(int nn, const int *__restrict__ flag, const int *__
     }
 }
 
-// Merge consecutive near entries whose source ranges touch.
+// Merge consecutive near entries whose source ranges touch.  A merged range
+// whose bounding box touches the batch's box (closed boxes, with a relative
+// margin) may hold a source that coincides with a target: its begin index is
+// stored with bit 31 set, and the field kernels mask r = 0 pairs only there.
+__device__ __forceinline__ bool boxes_touch(const double *cb, const double *hb, const double *lo,
+                                            const double *hi) {
+#pragma unroll
+    for (int d = 0; d < 3; d++) {
+        double c = 0.5 * (lo[d] + hi[d]), h = 0.5 * (hi[d] - lo[d]);
+        double gap = fabs(cb[d] - c) - (hb[d] + h);
+        double tol = 1e-12 * (fabs(cb[d]) + fabs(c) + hb[d] + h) + 1e-300;
+        if (gap > tol) return false;
+    }
+    return true;
+}
+
 template <bool FILL>
 __global__ void merge_ranges(int nbatch, const int *__restrict__ near_off,
                              const int *__restrict__ near_list, const int *__restrict__ sbegin,
-                             const int *__restrict__ send, int *__restrict__ cnt,
-                             const int *__restrict__ rng_off, int2 *__restrict__ rng) {
+                             const int *__restrict__ send, const double *__restrict__ scenter,
+                             const double *__restrict__ shalf, const int *__restrict__ batch_node,
+                             const double *__restrict__ tcenter, const double *__restrict__ thalf,
+                             int *__restrict__ cnt, const int *__restrict__ rng_off,
+                             int2 *__restrict__ rng) {
     int b = blockIdx.x * blockDim.x + threadIdx.x;
     if (b >= nbatch) return;
+    const int bn = batch_node[b];
+    const double cb[3] = {tcenter[3L * bn], tcenter[3L * bn + 1], tcenter[3L * bn + 2]};
+    const double hb[3] = {thalf[3L * bn], thalf[3L * bn + 1], thalf[3L * bn + 2]};
     int k = 0;
-    int cb = -1, ce = -1;
-    for (int e = near_off[b]; e < near_off[b + 1]; e++) {
-        int c = near_list[e];
-        int nb = sbegin[c], ne = send[c];
-        if (cb >= 0 && nb == ce) {
+    int cb0 = -1, ce = -1;
+    double lo[3], hi[3];
+    for (int e = near_off[b]; e <= near_off[b + 1]; e++) {
+        int c = -1, nb = -1, ne = -1;
+        if (e < near_off[b + 1]) {
+            c = near_list[e];
+            nb = sbegin[c];
+            ne = send[c];
+        }
+        if (c >= 0 && cb0 >= 0 && nb == ce) {
             ce = ne;
         } else {
-            if (cb >= 0) {
-                if (FILL) rng[rng_off[b] + k] = make_int2(cb, ce);
+            if (cb0 >= 0) {
+                if (FILL) {
+                    int flag = boxes_touch(cb, hb, lo, hi) ? (int)0x80000000u : 0;
+                    rng[rng_off[b] + k] = make_int2(cb0 | flag, ce);
+                }
                 k++;
             }
-            cb = nb;
+            if (c < 0) break;
+            cb0 = nb;
             ce = ne;
+#pragma unroll
+            for (int d = 0; d < 3; d++) {
+                lo[d] = INFINITY;
+                hi[d] = -INFINITY;
+            }
         }
-    }
-    if (cb >= 0) {
-        if (FILL) rng[rng_off[b] + k] = make_int2(cb, ce);
-        k++;
+#pragma unroll
+        for (int d = 0; d < 3; d++) {
+            lo[d] = fmin(lo[d], scenter[3L * c + d] - shalf[3L * c + d]);
+            hi[d] = fmax(hi[d], scenter[3L * c + d] + shalf[3L * c + d]);
+        }
     }
     if (!FILL) cnt[b] = k;
 }
@@ -465,7 +523,7 @@ __global__ void batch_costs(int nbatch, const int *__restrict__ batch_node,
     int bn = batch_node[b];
     long long nb = tend[bn] - tbegin[bn];
     long long s = 0;
-    for (int e = rng_off[b]; e < rng_off[b + 1]; e++) s += rng[e].y - rng[e].x;
+    for (int e = rng_off[b]; e < rng_off[b + 1]; e++) s += rng[e].y - range_begin(rng[e]);
     cost_near[b] = nb * s;
     cost_far[b] = nb * (long long)(far_off[b + 1] - far_off[b]);
     bsize[b] = (int)nb;
@@ -539,12 +597,12 @@ int build_lists(Plan &p, cudaStream_t s) {
             (rc = tmp.alloc(&idx, nt)) || (rc = tmp.alloc(&total, 1)))
             break;
         cudaMemsetAsync(mark, 0, sizeof(int) * nt, s);
-        mark_leaves<<<(nnt + 255) / 256, 256, 0, s>>>(nnt, p.tgt.nchild, p.tgt.begin, mark);
-        nonzero_flags<<<(nt + 255) / 256, 256, 0, s>>>(mark, nt, flags);
+        launch(mark_leaves, (nnt + 255) / 256, 256, 0, s, nnt, p.tgt.nchild, p.tgt.begin, mark);
+        launch(nonzero_flags, (nt + 255) / 256, 256, 0, s, mark, nt, flags);
         if ((rc = exclusive_scan(flags, idx, nt, total, tmp, s))) break;
         if ((rc = sync_int(total, &p.nbatch))) break;
         if ((rc = ar.alloc(&p.batch_node, p.nbatch))) break;
-        compact_leaves<<<(nt + 255) / 256, 256, 0, s>>>(mark, idx, nt, p.batch_node);
+        launch(compact_leaves, (nt + 255) / 256, 256, 0, s, mark, idx, nt, p.batch_node);
 
         const int nb = p.nbatch;
         int *ncnt = nullptr, *fcnt = nullptr;
@@ -574,7 +632,7 @@ int build_lists(Plan &p, cudaStream_t s) {
         ta.far_list = nullptr;
         ta.node_flag = node_flag;
         ta.err = p.err_flag;
-        traverse<false><<<(nb + 63) / 64, 64, 0, s>>>(ta);
+        launch(traverse<false>, (nb + 63) / 64, 64, 0, s, ta);
         if ((rc = exclusive_scan(ncnt, p.near_off, nb, p.near_off + nb, tmp, s))) break;
         if ((rc = exclusive_scan(fcnt, p.far_off, nb, p.far_off + nb, tmp, s))) break;
         if ((rc = sync_int(p.near_off + nb, &p.near_total))) break;
@@ -583,7 +641,7 @@ int build_lists(Plan &p, cudaStream_t s) {
             break;
         ta.near_list = p.near_list;
         ta.far_list = p.far_list;
-        traverse<true><<<(nb + 63) / 64, 64, 0, s>>>(ta);
+        launch(traverse<true>, (nb + 63) / 64, 64, 0, s, ta);
         int h_err = 0;
         if ((rc = sync_int(p.err_flag, &h_err))) break;
         if (h_err) { rc = set_error(TAGI_ERR_DEVICE, "source tree deeper than the traversal stack"); break; }
@@ -594,30 +652,32 @@ int build_lists(Plan &p, cudaStream_t s) {
         if ((rc = exclusive_scan(node_flag, sidx, nns, total, tmp, s))) break;
         if ((rc = sync_int(total, &p.nslots))) break;
         if ((rc = ar.alloc(&p.node_slot, nns)) || (rc = ar.alloc(&p.slot_node, p.nslots))) break;
-        assign_slots<<<(nns + 255) / 256, 256, 0, s>>>(nns, node_flag, sidx, p.node_slot, p.slot_node);
+        launch(assign_slots, (nns + 255) / 256, 256, 0, s, nns, node_flag, sidx, p.node_slot, p.slot_node);
         if ((rc = ar.alloc(&p.slot_geom, 6L * p.nslots))) break;
         if (p.nslots)
-            slot_geometry<<<(p.nslots + 127) / 128, 128, 0, s>>>(p.nslots, p.slot_node, p.src.center,
+            launch(slot_geometry, (p.nslots + 127) / 128, 128, 0, s, p.nslots, p.slot_node, p.src.center,
                                                                  p.src.half, p.slot_geom);
 
         // Merged near ranges.
         int *rcnt = nullptr;
         if ((rc = tmp.alloc(&rcnt, nb))) break;
         if ((rc = ar.alloc(&p.rng_off, nb + 1))) break;
-        merge_ranges<false><<<(nb + 127) / 128, 128, 0, s>>>(nb, p.near_off, p.near_list, p.src.begin,
-                                                             p.src.end, rcnt, nullptr, nullptr);
+        launch(merge_ranges<false>, (nb + 127) / 128, 128, 0, s, nb, p.near_off, p.near_list, p.src.begin,
+               p.src.end, p.src.center, p.src.half, p.batch_node, p.tgt.center, p.tgt.half, rcnt,
+               nullptr, nullptr);
         if ((rc = exclusive_scan(rcnt, p.rng_off, nb, p.rng_off + nb, tmp, s))) break;
         if ((rc = sync_int(p.rng_off + nb, &p.rng_total))) break;
         if ((rc = ar.alloc(&p.rng, p.rng_total))) break;
-        merge_ranges<true><<<(nb + 127) / 128, 128, 0, s>>>(nb, p.near_off, p.near_list, p.src.begin,
-                                                            p.src.end, nullptr, p.rng_off, p.rng);
+        launch(merge_ranges<true>, (nb + 127) / 128, 128, 0, s, nb, p.near_off, p.near_list, p.src.begin,
+               p.src.end, p.src.center, p.src.half, p.batch_node, p.tgt.center, p.tgt.half, nullptr,
+               p.rng_off, p.rng);
 
         // Upward-pass work items.
         if ((rc = ar.alloc(&p.slot_item_off, p.nslots + 1))) break;
         if (p.nslots) {
             int *nch = nullptr;
             if ((rc = tmp.alloc(&nch, p.nslots))) break;
-            slot_chunks<<<(p.nslots + 127) / 128, 128, 0, s>>>(p.nslots, p.slot_node, p.src.begin,
+            launch(slot_chunks, (p.nslots + 127) / 128, 128, 0, s, p.nslots, p.slot_node, p.src.begin,
                                                                p.src.end, P2M_CHUNK, nch);
             if ((rc = exclusive_scan(nch, p.slot_item_off, p.nslots, p.slot_item_off + p.nslots, tmp, s)))
                 break;
@@ -630,7 +690,7 @@ int build_lists(Plan &p, cudaStream_t s) {
             (rc = ar.alloc(&p.item_end, p.nitems)))
             break;
         if (p.nslots)
-            fill_items<<<(p.nslots + 127) / 128, 128, 0, s>>>(p.nslots, p.slot_node, p.src.begin,
+            launch(fill_items, (p.nslots + 127) / 128, 128, 0, s, p.nslots, p.slot_node, p.src.begin,
                                                               p.src.end, P2M_CHUNK, p.slot_item_off,
                                                               p.item_slot, p.item_begin, p.item_end);
 
@@ -638,7 +698,7 @@ int build_lists(Plan &p, cudaStream_t s) {
         long long *cn = nullptr, *cf = nullptr;
         int *bsz = nullptr;
         if ((rc = tmp.alloc(&cn, nb)) || (rc = tmp.alloc(&cf, nb)) || (rc = tmp.alloc(&bsz, nb))) break;
-        batch_costs<<<(nb + 127) / 128, 128, 0, s>>>(nb, p.batch_node, p.tgt.begin, p.tgt.end,
+        launch(batch_costs, (nb + 127) / 128, 128, 0, s, nb, p.batch_node, p.tgt.begin, p.tgt.end,
                                                      p.rng_off, p.rng, p.far_off, cn, cf, bsz);
         std::vector<long long> hcn(nb), hcf(nb);
         std::vector<int> hsz(nb);

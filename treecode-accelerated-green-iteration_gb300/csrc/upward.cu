@@ -126,11 +126,6 @@ __global__ void p2m_reduce(const double *__restrict__ part, const int *__restric
     }
 }
 
-__global__ void to_float(const double *__restrict__ a, float *__restrict__ b, long n) {
-    long i = (long)blockIdx.x * blockDim.x + threadIdx.x;
-    if (i < n) b[i] = (float)a[i];
-}
-
 template <typename T>
 int launch_p2m(Plan &p, const T *q, long q_stride, int norb, double *part, cudaStream_t s) {
     P2MArgs<T> a;
@@ -154,12 +149,12 @@ int launch_p2m(Plan &p, const T *q, long q_stride, int norb, double *part, cudaS
     if (p.n1 <= 8) {
         if (smem > 48 * 1024)
             cudaFuncSetAttribute(p2m_kernel<T, 8>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-        p2m_kernel<T, 8><<<grid, P2M_THREADS, smem, s>>>(a);
+        launch(p2m_kernel<T, 8>, grid, P2M_THREADS, smem, s, a);
     } else {
         if (smem > 48 * 1024)
             cudaFuncSetAttribute(p2m_kernel<T, MAX_DEGREE + 1>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                  (int)smem);
-        p2m_kernel<T, MAX_DEGREE + 1><<<grid, P2M_THREADS, smem, s>>>(a);
+        launch(p2m_kernel<T, MAX_DEGREE + 1>, grid, P2M_THREADS, smem, s, a);
     }
     TAGI_LAUNCH_CHECK();
     return TAGI_OK;
@@ -167,24 +162,46 @@ int launch_p2m(Plan &p, const T *q, long q_stride, int norb, double *part, cudaS
 
 }  // namespace
 
+// Weight modified charges (q = w).  The mixed path uses charges built with
+// the same FP32 products as its charge vectors, so qhat - f_i what keeps the
+// subtraction's structure; the FP64 set is built on first use by an FP64 call.
 int build_weight_charges(Plan &p, cudaStream_t s) {
-    TAGI_TRY(p.arena.alloc(&p.what64, (size_t)p.nslots * p.P));
     TAGI_TRY(p.arena.alloc(&p.what32, (size_t)p.nslots * p.P));
+    p.what64_ready = false;
     if (p.nslots == 0) return TAGI_OK;
     Arena tmp;
     tmp.stream = s;
     double *part = nullptr;
     int rc = tmp.alloc(&part, (size_t)p.nitems * p.P);
-    if (!rc) rc = launch_p2m<double>(p, p.sw64, p.src.n, 1, part, s);
+    if (!rc) rc = launch_p2m<float>(p, p.sw32, p.src.n, 1, part, s);
     if (!rc) {
-        p2m_reduce<double><<<dim3(p.nslots, 1), 256, 0, s>>>(part, p.slot_item_off, p.nslots, p.nitems,
-                                                             p.P, p.what64);
-        long tot = (long)p.nslots * p.P;
-        to_float<<<(unsigned)((tot + 255) / 256), 256, 0, s>>>(p.what64, p.what32, tot);
+        launch(p2m_reduce<float>, dim3(p.nslots, 1), 256, 0, s, part, p.slot_item_off, p.nslots, p.nitems, p.P,
+               p.what32);
         if (cudaGetLastError() != cudaSuccess) rc = set_error(TAGI_ERR_CUDA, "weight charge kernels");
     }
     tmp.release();
     return rc;
+}
+
+int ensure_weight_charges64(Plan &p, cudaStream_t s) {
+    if (p.what64_ready) return TAGI_OK;
+    if (!p.what64) TAGI_TRY(p.arena.alloc(&p.what64, (size_t)p.nslots * p.P));
+    if (p.nslots) {
+        Arena tmp;
+        tmp.stream = s;
+        double *part = nullptr;
+        int rc = tmp.alloc(&part, (size_t)p.nitems * p.P);
+        if (!rc) rc = launch_p2m<double>(p, p.sw64, p.src.n, 1, part, s);
+        if (!rc) {
+            launch(p2m_reduce<double>, dim3(p.nslots, 1), 256, 0, s, part, p.slot_item_off, p.nslots, p.nitems,
+                   p.P, p.what64);
+            if (cudaGetLastError() != cudaSuccess) rc = set_error(TAGI_ERR_CUDA, "weight charge kernels");
+        }
+        tmp.release();
+        if (rc) return rc;
+    }
+    p.what64_ready = true;
+    return TAGI_OK;
 }
 
 // Charges for norb sorted charge vectors already in p.q32 / p.q64.
@@ -192,11 +209,11 @@ int modified_charges(Plan &p, int precision, int norb, cudaStream_t s) {
     if (p.nslots == 0) return TAGI_OK;
     if (precision == PREC_MIXED) {
         TAGI_TRY(launch_p2m<float>(p, p.q32, p.src.n, norb, p.part, s));
-        p2m_reduce<float><<<dim3(p.nslots, norb), 256, 0, s>>>(p.part, p.slot_item_off, p.nslots,
+        launch(p2m_reduce<float>, dim3(p.nslots, norb), 256, 0, s, p.part, p.slot_item_off, p.nslots,
                                                                p.nitems, p.P, p.qhat32);
     } else {
         TAGI_TRY(launch_p2m<double>(p, p.q64, p.src.n, norb, p.part, s));
-        p2m_reduce<double><<<dim3(p.nslots, norb), 256, 0, s>>>(p.part, p.slot_item_off, p.nslots,
+        launch(p2m_reduce<double>, dim3(p.nslots, norb), 256, 0, s, p.part, p.slot_item_off, p.nslots,
                                                                 p.nitems, p.P, p.qhat64);
     }
     TAGI_LAUNCH_CHECK();
