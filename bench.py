@@ -227,9 +227,9 @@ def reference_arm(args):
 # ---------------------------------------------------------------------------
 # GB300 arm
 # ---------------------------------------------------------------------------
-def profile_traffic(label):
-    """DRAM bytes per launch of the dominant kernel from the committed ncu summary."""
-    path = os.path.join(ROOT, "profiles", f"near_field_{label}_1.5M.md")
+def profile_traffic(kernel, label):
+    """DRAM bytes per launch of a field kernel from the committed ncu summary."""
+    path = os.path.join(ROOT, "profiles", f"{kernel}_field_{label}_1.5M.md")
     if not os.path.exists(path):
         return None
     for line in open(path):
@@ -335,7 +335,7 @@ def gb300_arm(args):
     nat.check(L.tagi_pair_peak(int(wl["kernel"]), int(wl["singularity"]),
                                0 if dominant == "near" else 1, kp0, ctypes.byref(peak),
                                ctypes.c_void_p(stream.cuda_stream)))
-    traffic = profile_traffic(wl["label"]) if dominant == "near" else None
+    traffic = profile_traffic(dominant, wl["label"])
     roofline = {"bound": "mufu", "achieved": achieved / 1e9, "peak": peak.value / 1e9,
                 "unit": "Gpair/s", "frac": achieved / peak.value, "traffic": traffic,
                 "kernel": f"{dominant}_mixed ({wl['label']})",
