@@ -163,6 +163,18 @@ int tagi_direct_dev(int numTargets, const double *targetX, const double *targetY
 int tagi_mgs_dev(double *V, double *U, const double *W, int targetWavefunction, int numPoints,
                  int numWavefunctions, void *stream);
 
+/* Same work as tagi_mgs_dev, but the call allocates no device memory: for
+ * callers that cannot allocate while they run (device memory handed to
+ * another allocator or held to a fixed budget, or a loop in which a
+ * cudaMalloc/cudaFree would synchronize the device).  No counterpart in the
+ * reference.  Its scratch is a fixed ~1.06 MB device array that every GPU
+ * loading this library keeps until exit; targetWavefunction may be at most
+ * 128 (larger requests return TAGI_ERR_ARG).  The first call on a device
+ * looks the array's address up (make it before any stream capture); all calls
+ * share the array, so calls that overlap on the GPU race. */
+int tagi_mgs_dev_noalloc(double *V, double *U, const double *W, int targetWavefunction,
+                         int numPoints, int numWavefunctions, void *stream);
+
 /* Device form of InterpolateBetweenTwoMeshes (TwoMeshInterpolation.c:163);
  * the points-per-cell arrays are device int32 arrays. */
 int tagi_interp_dev(const double *coarseX, const double *coarseY, const double *coarseZ,

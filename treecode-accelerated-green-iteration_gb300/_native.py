@@ -41,6 +41,7 @@ SIGNATURES = {
     "tagi_direct_dev": (_i, [_i, _vp, _vp, _vp, _vp, _i, _vp, _i, _vp, _vp, _vp, _vp, _vp, _vp, _i,
                              _dp, _i, _vp]),
     "tagi_mgs_dev": (_i, [_vp, _vp, _vp, _i, _i, _i, _vp]),
+    "tagi_mgs_dev_noalloc": (_i, [_vp, _vp, _vp, _i, _i, _i, _vp]),
     "tagi_interp_dev": (_i, [_vp, _vp, _vp, _vp, _vp, _i, _vp, _vp, _vp, _vp, _vp, _i, _i, _i, _vp]),
     "tagi_set_precision": (_i, [_i]),
     "tagi_get_precision": (_i, []),

@@ -10,6 +10,9 @@
 // summed in block order, so results do not depend on scheduling.
 #include "tagi_internal.h"
 
+#include <algorithm>
+#include <mutex>
+
 namespace tagi {
 
 namespace {
@@ -142,3 +145,100 @@ int mgs_device(double *V, double *U, const double *W, int target, int npts, int 
 }
 
 }  // namespace tagi
+
+// ---------------------------------------------------------------------------
+// Weighted Gram-Schmidt without any device allocation.
+//
+// Some callers cannot allocate device memory while they run: a process whose
+// device memory is handed entirely to another allocator (a framework's caching
+// pool, a fixed per-job budget), or a latency-critical Green-iteration loop in
+// which a cudaMalloc/cudaFree would synchronize the device and stall other
+// streams.  tagi_mgs_dev_noalloc does the same work as tagi_mgs_dev with its
+// scratch (per-block partial sums, projection coefficients, norm partials) in
+// the fixed device array below instead of freshly allocated memory.
+//
+// * The array is MGS_NOALLOC_BLOCKS x (MGS_NOALLOC_ROWS + 1) + MGS_NOALLOC_ROWS
+//   doubles (about 1.06 MB); every GPU that loads this library holds it until
+//   the process exits.  Requests with targetWavefunction > MGS_NOALLOC_ROWS are
+//   rejected with TAGI_ERR_ARG.
+// * Host code cannot use the array's name as a device address: the first call
+//   on each device (with that device current) looks the address up with
+//   cudaGetSymbolAddress and keeps it.  Make that first call before any stream
+//   capture.
+// * All calls share the array and it keeps the last call's contents.  Every
+//   entry a call reads is written earlier in the same call, so nothing needs
+//   clearing; two calls that overlap on the GPU (different streams, or
+//   different host threads on one device) race on it.
+// ---------------------------------------------------------------------------
+namespace tagi {
+namespace {
+
+constexpr int MGS_NOALLOC_BLOCKS = 1024;
+constexpr int MGS_NOALLOC_ROWS = 128;
+constexpr long MGS_NOALLOC_DOUBLES =
+    (long)MGS_NOALLOC_BLOCKS * (MGS_NOALLOC_ROWS + 1) + MGS_NOALLOC_ROWS;
+
+static __device__ __align__(256) double g_mgs_noalloc_scratch[MGS_NOALLOC_DOUBLES];
+
+std::mutex g_mgs_noalloc_mu;
+double *g_mgs_noalloc_ptr[64] = {};
+
+int mgs_noalloc_scratch(double **out) {
+    int dev = 0;
+    TAGI_CUDA(cudaGetDevice(&dev));
+    if (dev < 0 || dev >= 64) return set_error(TAGI_ERR_DEVICE, "device ordinal %d out of range", dev);
+    std::lock_guard<std::mutex> lk(g_mgs_noalloc_mu);
+    if (!g_mgs_noalloc_ptr[dev]) {
+        void *p = nullptr;
+        cudaError_t e = cudaGetSymbolAddress(&p, g_mgs_noalloc_scratch);
+        if (e != cudaSuccess || !p)
+            return set_error(TAGI_ERR_CUDA, "cudaGetSymbolAddress of the MGS scratch array failed: %s",
+                             cudaGetErrorString(e));
+        g_mgs_noalloc_ptr[dev] = static_cast<double *>(p);
+    }
+    *out = g_mgs_noalloc_ptr[dev];
+    return TAGI_OK;
+}
+
+}  // namespace
+
+}  // namespace tagi
+
+extern "C" int tagi_mgs_dev_noalloc(double *V, double *U, const double *W, int targetWavefunction,
+                                    int numPoints, int numWavefunctions, void *stream) {
+    using namespace tagi;
+    if (numPoints < 0 || numWavefunctions < 1) return set_error(TAGI_ERR_ARG, "bad MGS sizes");
+    if (targetWavefunction < 0 || targetWavefunction >= numWavefunctions)
+        return set_error(TAGI_ERR_ARG, "targetWavefunction %d outside [0, %d)", targetWavefunction,
+                         numWavefunctions);
+    if (targetWavefunction > MGS_NOALLOC_ROWS)
+        return set_error(TAGI_ERR_ARG,
+                         "tagi_mgs_dev_noalloc handles targetWavefunction <= %d (got %d); use tagi_mgs_dev",
+                         MGS_NOALLOC_ROWS, targetWavefunction);
+    if (numPoints == 0) return TAGI_OK;
+    if (!V || !U || !W) return set_error(TAGI_ERR_ARG, "null device pointer");
+    cudaStream_t s = (cudaStream_t)stream;
+    double *scratch = nullptr;
+    TAGI_TRY(mgs_noalloc_scratch(&scratch));
+    int dev = 0, sms = 0;
+    TAGI_CUDA(cudaGetDevice(&dev));
+    TAGI_CUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
+    long nblk = std::min(4L * sms, (long)MGS_NOALLOC_BLOCKS);
+    long chunk = ((long)numPoints + nblk - 1) / nblk;
+    chunk = ((chunk + MT - 1) / MT) * MT;
+    nblk = ((long)numPoints + chunk - 1) / chunk;
+    const int target = targetWavefunction;
+    double *partial = scratch;                                   // [nblk][target]
+    double *r = scratch + (long)MGS_NOALLOC_BLOCKS * MGS_NOALLOC_ROWS;   // [target]
+    double *npart = r + MGS_NOALLOC_ROWS;                        // [nblk]
+    if (target > 0) {
+        dim3 g((unsigned)nblk, (unsigned)((target + RB - 1) / RB));
+        launch(mgs_dots, g, MT, 0, s, V, U, W, target, (long)numPoints, chunk, partial);
+        launch(mgs_reduce_rows, (target + 127) / 128, 128, 0, s, partial, (int)nblk, target, r);
+    }
+    launch(mgs_subtract, (unsigned)nblk, MT, 0, s, V, U, W, r, target, (long)numPoints, chunk, npart);
+    launch(mgs_normalize, (unsigned)nblk, MT, 0, s, V, U, npart, (int)nblk, target, (long)numPoints, chunk);
+    TAGI_LAUNCH_CHECK();
+    return TAGI_OK;
+}
+
