@@ -132,9 +132,10 @@ int tagi_plan_convolve(tagi_plan *plan, int numOrbitals, const double *targetVal
                        int numberOfKernelParameters, const double *kernelParameters,
                        int singularity, int precision, void *stream);
 
-/* Plan statistics: info[0..11] = source nodes, target nodes, batches,
+/* Plan statistics: info[0..12] = source nodes, target nodes, batches,
  * near-list entries, far-list entries, slots, proxy points P, upward items,
- * merged near ranges, largest batch, near pairs, far pairs (per orbital). */
+ * merged near ranges, largest batch, near pairs, far pairs, near pairs in
+ * close ranges (pair counts per orbital). */
 int tagi_plan_info(const tagi_plan *plan, double *info);
 
 /* Copies of the plan's integer structure to HOST arrays, for parity checks.
@@ -194,9 +195,9 @@ int tagi_beta_parameters(double beta, double *theta, int *degree, int *sourceLea
 /* Instrumentation: number of kernels this library has launched in this
  * process; optional per-phase device timing with CUDA events on the
  * launching stream.  Phases: 0 tree, 1 lists, 2 upward pass, 3 near field,
- * 4 far field, 5 glue.  tagi_profile_read waits for the recorded events,
- * returns summed milliseconds and mark counts per phase (nphase >= 6), and
- * clears the record. */
+ * 4 far field, 5 glue, 6 near field close-range pass.  tagi_profile_read
+ * waits for the recorded events, returns summed milliseconds and mark
+ * counts per phase (nphase >= 7), and clears the record. */
 long long tagi_launch_count(void);
 /* Pair-throughput ceiling of the mixed-precision field kernels on this GPU:
  * their inner-loop arithmetic (variant 0: near-field loop, 1: far-field

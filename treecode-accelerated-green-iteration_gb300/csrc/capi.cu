@@ -107,6 +107,23 @@ __global__ void gather_weights(const double *__restrict__ w, const int *__restri
     w32[i] = (float)v;
 }
 
+// FP32 hi/lo split of each sorted point's coordinates (hi + lo = x to ~2^-48).
+__global__ void split_points(const double *__restrict__ x, const double *__restrict__ y,
+                             const double *__restrict__ z, int n, float4 *__restrict__ hi,
+                             float4 *__restrict__ lo) {
+    long i = (long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    const double v[3] = {x[i], y[i], z[i]};
+    float h[3], l[3];
+#pragma unroll
+    for (int d = 0; d < 3; d++) {
+        h[d] = (float)v[d];
+        l[d] = (float)(v[d] - (double)h[d]);
+    }
+    hi[i] = make_float4(h[0], h[1], h[2], 0.f);
+    lo[i] = make_float4(l[0], l[1], l[2], 0.f);
+}
+
 // SS term only (no sources): phi_i = f_i * 4pi/k^2 or f_i * 2pi/a^2.
 __global__ void ss_only(const double *__restrict__ tv, int nt, double c, double *__restrict__ out) {
     long i = (long)blockIdx.x * blockDim.x + threadIdx.x;
@@ -144,7 +161,7 @@ int plan_create(Plan **out, int nt, const double *tx, const double *ty, const do
     for (int m = 0; m <= MAX_DEGREE; m++) p->cheb[m] = m <= degree ? std::cos(M_PI * (double)m / (double)degree) : 0.0;
     int rc = TAGI_OK;
     do {
-        if ((rc = p->arena.alloc(&p->queue, 2)) || (rc = p->arena.alloc(&p->err_flag, 1))) break;
+        if ((rc = p->arena.alloc(&p->queue, 3)) || (rc = p->arena.alloc(&p->err_flag, 1))) break;
         cudaMemsetAsync(p->err_flag, 0, sizeof(int), s);
         phase_mark(PH_TREE, true, s);
         if ((rc = build_tree(p->src, sx, sy, sz, ns, sl, p->arena, p->err_flag, s))) break;
@@ -153,6 +170,11 @@ int plan_create(Plan **out, int nt, const double *tx, const double *ty, const do
         phase_mark(PH_LISTS, true, s);
         if ((rc = p->arena.alloc(&p->sw64, ns)) || (rc = p->arena.alloc(&p->sw32, ns))) break;
         launch(gather_weights, (ns + 255) / 256, 256, 0, s, sw, p->src.perm, ns, p->sw64, p->sw32);
+        if ((rc = p->arena.alloc(&p->src_hi, ns)) || (rc = p->arena.alloc(&p->src_lo, ns)) ||
+            (rc = p->arena.alloc(&p->tgt_hi, nt)) || (rc = p->arena.alloc(&p->tgt_lo, nt)))
+            break;
+        launch(split_points, (ns + 255) / 256, 256, 0, s, p->src.x, p->src.y, p->src.z, ns, p->src_hi, p->src_lo);
+        launch(split_points, (nt + 255) / 256, 256, 0, s, p->tgt.x, p->tgt.y, p->tgt.z, nt, p->tgt_hi, p->tgt_lo);
         if ((rc = build_lists(*p, s))) break;
         if ((rc = build_weight_charges(*p, s))) break;
         phase_mark(PH_LISTS, false, s);
@@ -379,9 +401,10 @@ int tagi_plan_convolve(tagi_plan *plan, int numOrbitals, const double *targetVal
 int tagi_plan_info(const tagi_plan *plan, double *info) {
     if (!plan || !info) return set_error(TAGI_ERR_ARG, "null pointer");
     const Plan &p = *reinterpret_cast<const Plan *>(plan);
-    double v[12] = {(double)p.src.nnodes, (double)p.tgt.nnodes, (double)p.nbatch, (double)p.near_total,
+    double v[13] = {(double)p.src.nnodes, (double)p.tgt.nnodes, (double)p.nbatch, (double)p.near_total,
                     (double)p.far_total, (double)p.nslots, (double)p.P, (double)p.nitems,
-                    (double)p.rng_total, (double)p.max_batch, p.near_pairs, p.far_pairs};
+                    (double)p.rng_total, (double)p.max_batch, p.near_pairs, p.far_pairs,
+                    p.near_close_pairs};
     memcpy(info, v, sizeof(v));
     return TAGI_OK;
 }

@@ -64,7 +64,9 @@ struct Fields {
     // near side
     const int *rng_off;
     const int2 *rng;
+    const float *rng_dmin;
     const double *sx, *sy, *sz;
+    const float4 *shi, *slo, *thi, *tlo;  // FP32 hi/lo splits of absolute coordinates
     int ns;
     const float *q32, *w32;       // [norb][ns] charges f*w, [ns] weights
     const double *f64, *w64;      // [norb][ns] values f, [ns] weights
@@ -97,11 +99,10 @@ __device__ __forceinline__ int next_item(int *queue, int *s_item) {
     return *s_item;
 }
 
-// One pair in scaled coordinates; MASK drops the coincident (r = 0) pair.
+// One pair from its squared scaled distance r2 = r'^2; MASK drops the
+// coincident (r = 0) pair.
 template <int KERN, bool SS, bool MASK>
-__device__ __forceinline__ float pair_scaled(float dx, float dy, float dz, float q, float w, float fi,
-                                             float acc) {
-    const float r2 = fmaf(dx, dx, fmaf(dy, dy, dz * dz));
+__device__ __forceinline__ float pair_r2(float r2, float q, float w, float fi, float acc) {
     float rinv = rsqrt_mufu(r2);
     if (MASK) rinv = r2 > 0.f ? rinv : 0.f;
     if (KERN == KERNEL_YUKAWA) {
@@ -113,6 +114,12 @@ __device__ __forceinline__ float pair_scaled(float dx, float dy, float dz, float
     } else {
         return fmaf(rinv, q, acc);
     }
+}
+
+template <int KERN, bool SS, bool MASK>
+__device__ __forceinline__ float pair_scaled(float dx, float dy, float dz, float q, float w, float fi,
+                                             float acc) {
+    return pair_r2<KERN, SS, MASK>(fmaf(dx, dx, fmaf(dy, dy, dz * dz)), q, w, fi, acc);
 }
 
 // Compensated (Kahan) addition of an FP32 partial into (sum, cmp).
@@ -127,63 +134,100 @@ __device__ __forceinline__ void kahan_add(float &sum, float &cmp, float part) {
 // KCHUNK and each chunk is added to the target's Kahan sum: a long FP32 run
 // loses ~sqrt(n) u of its total, and singularity subtraction multiplies that
 // loss by |f_i int G| / |phi_i| (often 10-100).
+// Ordinary tiles: s_a[j] = (scaled batch-relative x, y, z, q), s_b[j].w = w.
+// PRECISE tiles (close ranges): s_a[j] = (x_hi, y_hi, z_hi, q) and
+// s_b[j] = (x_lo, y_lo, z_lo, w) are FP32 splits of the absolute FP64
+// coordinates, the targets likewise; each difference is (t_hi - s_hi) +
+// (t_lo - s_lo) -- exact hi differences for nearby points -- and the unscaled
+// r^2 is multiplied by sc2 = sc^2, so the shortest pairs keep FP32 relative
+// precision in r whatever the batch size.
 constexpr int KCHUNK = 64;
-template <int KERN, bool SS, bool MASK, int NT>
-__device__ __forceinline__ void near_tile(const float4 *__restrict__ s_src, const float *__restrict__ s_w,
+template <int KERN, bool SS, bool MASK, bool PRECISE, int NT>
+__device__ __forceinline__ void near_tile(const float4 *__restrict__ s_a, const float4 *__restrict__ s_b,
                                           int cnt, const float (&tx)[NT], const float (&ty)[NT],
-                                          const float (&tz)[NT], const float (&fi)[NT], float (&sum)[NT],
-                                          float (&cmp)[NT]) {
-    if (cnt == NTILE) {
-#pragma unroll 1
-        for (int j0 = 0; j0 < NTILE; j0 += KCHUNK) {
-            float part[NT];
+                                          const float (&tz)[NT], const float *__restrict__ s_tl, float sc2,
+                                          const float (&fi)[NT], float (&sum)[NT], float (&cmp)[NT]) {
+    // lo parts of this thread's targets (only live inside PRECISE tiles)
+    float lx[NT], ly[NT], lz[NT];
 #pragma unroll
-            for (int k = 0; k < NT; k++) part[k] = 0.f;
+    for (int k = 0; k < NT; k++) {
+        lx[k] = PRECISE ? s_tl[3 * k] : 0.f;
+        ly[k] = PRECISE ? s_tl[3 * k + 1] : 0.f;
+        lz[k] = PRECISE ? s_tl[3 * k + 2] : 0.f;
+    }
+    for (int j0 = 0; j0 < cnt; j0 += KCHUNK) {
+        const int j1 = min(j0 + KCHUNK, cnt);
+        float part[NT];
+#pragma unroll
+        for (int k = 0; k < NT; k++) part[k] = 0.f;
+        if (j1 - j0 == KCHUNK) {
 #pragma unroll 8
             for (int j = j0; j < j0 + KCHUNK; j++) {
-                const float4 sj = s_src[j];
-                const float w = s_w[j];
+                const float4 sa = s_a[j];
+                if (PRECISE) {
+                    const float4 sb = s_b[j];
 #pragma unroll
-                for (int k = 0; k < NT; k++)
-                    part[k] = pair_scaled<KERN, SS, MASK>(tx[k] - sj.x, ty[k] - sj.y, tz[k] - sj.z, sj.w, w,
+                    for (int k = 0; k < NT; k++) {
+                        const float dx = (tx[k] - sa.x) + (lx[k] - sb.x);
+                        const float dy = (ty[k] - sa.y) + (ly[k] - sb.y);
+                        const float dz = (tz[k] - sa.z) + (lz[k] - sb.z);
+                        part[k] = pair_r2<KERN, SS, MASK>(fmaf(dx, dx, fmaf(dy, dy, dz * dz)) * sc2, sa.w, sb.w,
                                                           fi[k], part[k]);
+                    }
+                } else {
+                    const float w = s_b[j].w;
+#pragma unroll
+                    for (int k = 0; k < NT; k++)
+                        part[k] = pair_scaled<KERN, SS, MASK>(tx[k] - sa.x, ty[k] - sa.y, tz[k] - sa.z, sa.w, w,
+                                                              fi[k], part[k]);
+                }
             }
-#pragma unroll
-            for (int k = 0; k < NT; k++) kahan_add(sum[k], cmp[k], part[k]);
-        }
-    } else {
-        for (int j0 = 0; j0 < cnt; j0 += KCHUNK) {
-            const int j1 = min(j0 + KCHUNK, cnt);
-            float part[NT];
-#pragma unroll
-            for (int k = 0; k < NT; k++) part[k] = 0.f;
-#pragma unroll 4
+        } else {
+#pragma unroll 2
             for (int j = j0; j < j1; j++) {
-                const float4 sj = s_src[j];
-                const float w = s_w[j];
+                const float4 sa = s_a[j];
+                const float4 sb = s_b[j];
 #pragma unroll
-                for (int k = 0; k < NT; k++)
-                    part[k] = pair_scaled<KERN, SS, MASK>(tx[k] - sj.x, ty[k] - sj.y, tz[k] - sj.z, sj.w, w,
-                                                          fi[k], part[k]);
+                for (int k = 0; k < NT; k++) {
+                    const float dx = PRECISE ? (tx[k] - sa.x) + (lx[k] - sb.x) : tx[k] - sa.x;
+                    const float dy = PRECISE ? (ty[k] - sa.y) + (ly[k] - sb.y) : ty[k] - sa.y;
+                    const float dz = PRECISE ? (tz[k] - sa.z) + (lz[k] - sb.z) : tz[k] - sa.z;
+                    const float r2 = fmaf(dx, dx, fmaf(dy, dy, dz * dz));
+                    part[k] = pair_r2<KERN, SS, MASK>(PRECISE ? r2 * sc2 : r2, sa.w, sb.w, fi[k], part[k]);
+                }
             }
-#pragma unroll
-            for (int k = 0; k < NT; k++) kahan_add(sum[k], cmp[k], part[k]);
         }
+#pragma unroll
+        for (int k = 0; k < NT; k++) kahan_add(sum[k], cmp[k], part[k]);
     }
+}
+
+// Split an FP64 value into FP32 hi + lo.
+__device__ __forceinline__ void split_f32(double v, float &hi, float &lo) {
+    hi = (float)v;
+    lo = (float)(v - (double)hi);
 }
 
 // ---------------------------------------------------------------------------
 // Near field, mixed precision.
 // ---------------------------------------------------------------------------
-template <int KERN, bool SS, int NT>
-__global__ void __launch_bounds__(FT, 3) near_mixed(Fields a) {
-    __shared__ float4 s_src[NTILE];
-    __shared__ float s_w[NTILE];
+// PASS 0 handles the ordinary near ranges, PASS 1 the close ones (double-float
+// coordinates, r = 0 mask) into a second output; two passes keep each
+// kernel's register footprint at two tile variants.
+#ifndef TAGI_NEAR_MINB
+#define TAGI_NEAR_MINB 3   // resident CTAs per SM the near kernel is compiled for
+#endif
+template <int KERN, bool SS, int NT, int PASS>
+__global__ void __launch_bounds__(FT, TAGI_NEAR_MINB) near_mixed(Fields a) {
+    __shared__ float4 s_a[NTILE];
+    __shared__ float4 s_b[NTILE];
+    __shared__ float s_tlo[FT * NT * 3];
     __shared__ int s_item;
     const int tid = threadIdx.x;
     const int total = a.nbatch * a.norb;
+    float *my_tl = s_tlo + 3 * NT * tid;
     for (;;) {
-        const int item = next_item(a.queue, &s_item);
+        const int item = next_item(a.queue + (PASS == 1 ? 2 : 0), &s_item);
         if (item >= total) break;
         const int b = a.order[item / a.norb];
         const int orb = item - (item / a.norb) * a.norb;
@@ -193,6 +237,7 @@ __global__ void __launch_bounds__(FT, 3) near_mixed(Fields a) {
                      cbz = a.tcenter[3L * bn + 2];
         const float scf = a.kc32[orb];
         const double sc = (double)scf;
+        const float sc2 = (float)(sc * sc);
         const float *q = a.q32 + (long)orb * a.ns;
         const float *ft = a.ft32 + (long)orb * a.nt;
         const int r0 = a.rng_off[b], r1 = a.rng_off[b + 1];
@@ -205,30 +250,64 @@ __global__ void __launch_bounds__(FT, 3) near_mixed(Fields a) {
             for (int k = 0; k < NT; k++) {
                 int i = base + NT * tid + k;
                 bool v = i < te;
-                tx[k] = v ? (float)(a.tx[i] - cbx) * scf : 0.f;
-                ty[k] = v ? (float)(a.ty[i] - cby) * scf : 0.f;
-                tz[k] = v ? (float)(a.tz[i] - cbz) * scf : 0.f;
+                if (PASS == 1) {
+                    const float4 h = v ? a.thi[i] : make_float4(0.f, 0.f, 0.f, 0.f);
+                    const float4 l = v ? a.tlo[i] : make_float4(0.f, 0.f, 0.f, 0.f);
+                    tx[k] = h.x;
+                    ty[k] = h.y;
+                    tz[k] = h.z;
+                    my_tl[3 * k] = l.x;
+                    my_tl[3 * k + 1] = l.y;
+                    my_tl[3 * k + 2] = l.z;
+                } else {
+                    tx[k] = v ? (float)((a.tx[i] - cbx) * sc) : 0.f;
+                    ty[k] = v ? (float)((a.ty[i] - cby) * sc) : 0.f;
+                    tz[k] = v ? (float)((a.tz[i] - cbz) * sc) : 0.f;
+                }
                 fi[k] = v ? ft[i] : 0.f;
                 sum[k] = 0.f;
                 cmp[k] = 0.f;
             }
             for (int e = r0; e < r1; e++) {
                 const int2 r = a.rng[e];
-                const bool mask = range_may_coincide(r);
+                const bool close = range_is_close(r);
+                if (close != (PASS == 1)) continue;
                 const int rb = range_begin(r);
+                // Ranges far enough away: Yukawa terms are exactly 0 in FP32
+                // (2^{-r'} with r' > 127 flushes to zero); the Coulomb Gaussian
+                // correction is below 2^-40 of its term and is left out.
+                const float dm = a.rng_dmin[e] * scf;
+                if (KERN == KERNEL_YUKAWA && dm > 127.f) continue;
+                const bool noexp = KERN == KERNEL_COULOMB && SS && dm * dm > 40.f;
                 for (int t0 = rb; t0 < r.y; t0 += NTILE) {
                     const int cnt = min(NTILE, r.y - t0);
                     __syncthreads();
                     for (int j = tid; j < cnt; j += FT) {
-                        int jj = t0 + j;
-                        s_src[j] = make_float4((float)(a.sx[jj] - cbx) * scf, (float)(a.sy[jj] - cby) * scf,
-                                               (float)(a.sz[jj] - cbz) * scf, q[jj]);
-                        s_w[j] = a.w32[jj];
+                        const int jj = t0 + j;
+                        float4 sa, sb;
+                        if (PASS == 1) {
+                            sa = a.shi[jj];
+                            sb = a.slo[jj];
+                        } else {
+                            sa.x = (float)((a.sx[jj] - cbx) * sc);
+                            sa.y = (float)((a.sy[jj] - cby) * sc);
+                            sa.z = (float)((a.sz[jj] - cbz) * sc);
+                            sb.x = sb.y = sb.z = 0.f;
+                        }
+                        sa.w = q[jj];
+                        sb.w = a.w32[jj];
+                        s_a[j] = sa;
+                        s_b[j] = sb;
                     }
                     __syncthreads();
                     if (!warp_busy) continue;
-                    if (mask) near_tile<KERN, SS, true, NT>(s_src, s_w, cnt, tx, ty, tz, fi, sum, cmp);
-                    else near_tile<KERN, SS, false, NT>(s_src, s_w, cnt, tx, ty, tz, fi, sum, cmp);
+                    if (PASS == 1)
+                        near_tile<KERN, SS, true, true, NT>(s_a, s_b, cnt, tx, ty, tz, my_tl, sc2, fi, sum, cmp);
+                    else if (noexp)
+                        near_tile<KERN, false, false, false, NT>(s_a, s_b, cnt, tx, ty, tz, my_tl, sc2, fi, sum,
+                                                                 cmp);
+                    else
+                        near_tile<KERN, SS, false, false, NT>(s_a, s_b, cnt, tx, ty, tz, my_tl, sc2, fi, sum, cmp);
                 }
             }
 #pragma unroll
@@ -378,6 +457,268 @@ __global__ void __launch_bounds__(FT, 2) far_mixed(Fields a) {
             for (int k = 0; k < NT; k++) {
                 const int i = base + NT * tid + k;
                 if (i < te) a.out[(long)orb * a.nt + i] = ((double)sum[k] - (double)cmp[k]) * sc;
+            }
+        }
+    }
+}
+
+// ---------------------------------------------------------------------------
+// Orbital-group kernels (Yukawa, mixed precision): one item = (batch, group of
+// OG orbitals).  Per pair the differences, r^2, rsqrt and r are computed once
+// for the group; each orbital then adds exp2(-k_o log2(e) r) * rinv * c.
+// Coordinates are translated to the batch center but not scaled (each orbital
+// has its own k).  Charges are staged [source][orbital] so four orbitals come
+// in one 16-byte shared-memory read.  Orbitals past the last one of the
+// request have zero charges and are not written.
+// ---------------------------------------------------------------------------
+constexpr int GTILE = 256;   // sources per group tile
+
+template <bool SS, bool MASK, bool PRECISE, int OG>
+__device__ __forceinline__ void group_tile(const float4 *__restrict__ s_xyzw, const float4 *__restrict__ s_lo,
+                                           const float4 *__restrict__ s_q4, int cnt, float tx, float ty,
+                                           float tz, float lx, float ly, float lz, const float (&fi)[OG],
+                                           const float (&kc)[OG], const float (&kl)[OG], float (&sum)[OG],
+                                           float (&cmp)[OG]) {
+    for (int j0 = 0; j0 < cnt; j0 += KCHUNK) {
+        const int j1 = min(j0 + KCHUNK, cnt);
+        float part[OG];
+#pragma unroll
+        for (int o = 0; o < OG; o++) part[o] = 0.f;
+#pragma unroll 2
+        for (int j = j0; j < j1; j++) {
+            const float4 sj = s_xyzw[j];
+            float dx = tx - sj.x, dy = ty - sj.y, dz = tz - sj.z;
+            if (PRECISE) {
+                const float4 sl = s_lo[j];
+                dx += lx - sl.x;
+                dy += ly - sl.y;
+                dz += lz - sl.z;
+            }
+            const float r2 = fmaf(dx, dx, fmaf(dy, dy, dz * dz));
+            float rinv = rsqrt_mufu(r2);
+            if (MASK) rinv = r2 > 0.f ? rinv : 0.f;
+            const float r = r2 * rinv;
+#pragma unroll
+            for (int o4 = 0; o4 < OG / 4; o4++) {
+                const float4 q4 = s_q4[j * (OG / 4) + o4];
+                const float qv[4] = {q4.x, q4.y, q4.z, q4.w};
+#pragma unroll
+                for (int u = 0; u < 4; u++) {
+                    const int o = 4 * o4 + u;
+                    // exponent -k log2(e) r with the constant split hi + lo
+                    const float g = ex2_mufu(fmaf(kc[o], r, kl[o] * r)) * rinv;
+                    part[o] = fmaf(g, SS ? fmaf(-fi[o], sj.w, qv[u]) : qv[u], part[o]);
+                }
+            }
+        }
+#pragma unroll
+        for (int o = 0; o < OG; o++) kahan_add(sum[o], cmp[o], part[o]);
+    }
+}
+
+template <bool SS, int OG, int PASS>
+__global__ void __launch_bounds__(FT, 2) near_group(Fields a) {
+    __shared__ float4 s_xyzw[GTILE];
+    __shared__ float4 s_lo[GTILE];
+    __shared__ float4 s_q4[GTILE * OG / 4];
+    __shared__ int s_item;
+    const int tid = threadIdx.x;
+    const int ngroups = (a.norb + OG - 1) / OG;
+    const int total = a.nbatch * ngroups;
+    for (;;) {
+        const int item = next_item(a.queue + (PASS == 1 ? 2 : 0), &s_item);
+        if (item >= total) break;
+        const int b = a.order[item / ngroups];
+        const int g0 = (item - (item / ngroups) * ngroups) * OG;
+        const int bn = a.batch_node[b];
+        const int tb = a.tbegin[bn], te = a.tend[bn];
+        const double cbx = a.tcenter[3L * bn], cby = a.tcenter[3L * bn + 1], cbz = a.tcenter[3L * bn + 2];
+        float kc[OG], kl[OG];
+        float kmin = 3.4e38f;
+#pragma unroll
+        for (int o = 0; o < OG; o++) {
+            const int orb = g0 + o;
+            const double k2 = orb < a.norb ? -a.kp64[orb] * LOG2E : 0.0;   // -k log2(e)
+            split_f32(k2, kc[o], kl[o]);
+            if (orb < a.norb) kmin = fminf(kmin, a.kc32[orb]);
+        }
+        const int r0 = a.rng_off[b], r1 = a.rng_off[b + 1];
+        for (int base = tb; base < te; base += FT) {
+            const int i = base + tid;
+            const bool v = i < te;
+            const bool warp_busy = base + (tid & ~31) < te;
+            float tx, ty, tz, lx = 0.f, ly = 0.f, lz = 0.f;
+            if (PASS == 1) {  // absolute hi/lo splits (see near_tile)
+                const float4 h = v ? a.thi[i] : make_float4(0.f, 0.f, 0.f, 0.f);
+                const float4 l = v ? a.tlo[i] : make_float4(0.f, 0.f, 0.f, 0.f);
+                tx = h.x; ty = h.y; tz = h.z;
+                lx = l.x; ly = l.y; lz = l.z;
+            } else {
+                tx = v ? (float)(a.tx[i] - cbx) : 0.f;
+                ty = v ? (float)(a.ty[i] - cby) : 0.f;
+                tz = v ? (float)(a.tz[i] - cbz) : 0.f;
+            }
+            float fi[OG], sum[OG], cmp[OG];
+#pragma unroll
+            for (int o = 0; o < OG; o++) {
+                const int orb = g0 + o;
+                fi[o] = (v && orb < a.norb) ? a.ft32[(long)orb * a.nt + i] : 0.f;
+                sum[o] = 0.f;
+                cmp[o] = 0.f;
+            }
+            for (int e = r0; e < r1; e++) {
+                const int2 r = a.rng[e];
+                if (a.rng_dmin[e] * kmin > 127.f) continue;  // every orbital's term is exactly 0
+                const bool close = range_is_close(r);
+                if (close != (PASS == 1)) continue;
+                const int rb = range_begin(r);
+                for (int t0 = rb; t0 < r.y; t0 += GTILE) {
+                    const int cnt = min(GTILE, r.y - t0);
+                    __syncthreads();
+                    for (int j = tid; j < cnt; j += FT) {
+                        const int jj = t0 + j;
+                        float4 sa, sb;
+                        if (PASS == 1) {
+                            sa = a.shi[jj];
+                            sb = a.slo[jj];
+                        } else {
+                            sa.x = (float)(a.sx[jj] - cbx);
+                            sa.y = (float)(a.sy[jj] - cby);
+                            sa.z = (float)(a.sz[jj] - cbz);
+                            sb.x = sb.y = sb.z = 0.f;
+                        }
+                        sa.w = a.w32[jj];
+                        sb.w = 0.f;
+                        s_xyzw[j] = sa;
+                        s_lo[j] = sb;
+                    }
+                    for (int k = tid; k < cnt * OG; k += FT) {
+                        const int j = k / OG, o = k - j * OG;
+                        const int orb = g0 + o;
+                        reinterpret_cast<float *>(s_q4)[k] = orb < a.norb ? a.q32[(long)orb * a.ns + t0 + j] : 0.f;
+                    }
+                    __syncthreads();
+                    if (!warp_busy) continue;
+                    if (PASS == 1)
+                        group_tile<SS, true, true, OG>(s_xyzw, s_lo, s_q4, cnt, tx, ty, tz, lx, ly, lz, fi, kc, kl,
+                                                       sum, cmp);
+                    else
+                        group_tile<SS, false, false, OG>(s_xyzw, s_lo, s_q4, cnt, tx, ty, tz, lx, ly, lz, fi, kc,
+                                                         kl, sum, cmp);
+                }
+            }
+            if (v) {
+#pragma unroll
+                for (int o = 0; o < OG; o++)
+                    if (g0 + o < a.norb) a.out[(long)(g0 + o) * a.nt + i] = (double)sum[o] - (double)cmp[o];
+            }
+        }
+    }
+}
+
+template <bool SS, int MAXN1, int OG>
+__global__ void __launch_bounds__(FT, 2) far_group(Fields a) {
+    constexpr int MAXP = MAXN1 * MAXN1 * MAXN1;
+    __shared__ float4 s_q4[MAXP * OG / 4];
+    __shared__ float s_w[MAXP];
+    __shared__ float s_p[3][MAXN1];
+    __shared__ int s_item;
+    const int tid = threadIdx.x;
+    const int n1 = a.n1, P = a.P;
+    const int ngroups = (a.norb + OG - 1) / OG;
+    const int total = a.nbatch * ngroups;
+    for (;;) {
+        const int item = next_item(a.queue + 1, &s_item);
+        if (item >= total) break;
+        const int b = a.order[item / ngroups];
+        const int g0 = (item - (item / ngroups) * ngroups) * OG;
+        const int f0 = a.far_off[b], f1 = a.far_off[b + 1];
+        if (f0 == f1) continue;
+        const int bn = a.batch_node[b];
+        const int tb = a.tbegin[bn], te = a.tend[bn];
+        const double cb[3] = {a.tcenter[3L * bn], a.tcenter[3L * bn + 1], a.tcenter[3L * bn + 2]};
+        float kc[OG], kl[OG];
+#pragma unroll
+        for (int o = 0; o < OG; o++) split_f32((g0 + o) < a.norb ? -a.kp64[g0 + o] * LOG2E : 0.0, kc[o], kl[o]);
+        for (int base = tb; base < te; base += FT) {
+            const int i = base + tid;
+            const bool v = i < te;
+            const bool warp_busy = base + (tid & ~31) < te;
+            const float tx = v ? (float)(a.tx[i] - cb[0]) : 0.f;
+            const float ty = v ? (float)(a.ty[i] - cb[1]) : 0.f;
+            const float tz = v ? (float)(a.tz[i] - cb[2]) : 0.f;
+            float fi[OG], sum[OG], cmp[OG];
+#pragma unroll
+            for (int o = 0; o < OG; o++) {
+                const int orb = g0 + o;
+                fi[o] = (v && orb < a.norb) ? a.ft32[(long)orb * a.nt + i] : 0.f;
+                sum[o] = 0.f;
+                cmp[o] = 0.f;
+            }
+            for (int e = f0; e < f1; e++) {
+                const int slot = a.node_slot[a.far_list[e]];
+                const double *gm = a.geom + 6L * slot;
+                __syncthreads();
+                for (int k = tid; k < P * OG; k += FT) {
+                    const int kk = k / OG, o = k - kk * OG;
+                    const int orb = g0 + o;
+                    reinterpret_cast<float *>(s_q4)[k] =
+                        orb < a.norb ? a.qhat32[((long)orb * a.nslots + slot) * P + kk] : 0.f;
+                }
+                for (int k = tid; k < P; k += FT) s_w[k] = a.what32[(long)slot * P + k];
+                if (tid < 3 * n1) {
+                    const int d = tid / n1, m = tid - d * n1;
+                    const double cbd = d == 0 ? cb[0] : (d == 1 ? cb[1] : cb[2]);
+                    s_p[d][m] = (float)((gm[d] + gm[3 + d] * a.tn[m]) - cbd);
+                }
+                __syncthreads();
+                if (!warp_busy) continue;
+                float dz2[MAXN1];
+#pragma unroll
+                for (int m = 0; m < MAXN1; m++) {
+                    const float d = tz - s_p[2][m < n1 ? m : 0];
+                    dz2[m] = d * d;
+                }
+                int idx = 0;
+                for (int k1 = 0; k1 < n1; k1++) {
+                    float part[OG];
+#pragma unroll
+                    for (int o = 0; o < OG; o++) part[o] = 0.f;
+                    const float dx = tx - s_p[0][k1];
+                    const float dx2 = dx * dx;
+                    for (int k2 = 0; k2 < n1; k2++) {
+                        const float dy = ty - s_p[1][k2];
+                        const float rxy = fmaf(dy, dy, dx2);
+#pragma unroll
+                        for (int k3 = 0; k3 < MAXN1; k3++) {
+                            if (k3 < n1) {
+                                const float r2 = rxy + dz2[k3];
+                                const float rinv = rsqrt_mufu(r2);
+                                const float rr = r2 * rinv;
+                                const float wk = s_w[idx + k3];
+#pragma unroll
+                                for (int o4 = 0; o4 < OG / 4; o4++) {
+                                    const float4 q4 = s_q4[(idx + k3) * (OG / 4) + o4];
+                                    const float qv[4] = {q4.x, q4.y, q4.z, q4.w};
+#pragma unroll
+                                    for (int u = 0; u < 4; u++) {
+                                        const int o = 4 * o4 + u;
+                                        const float g = ex2_mufu(fmaf(kc[o], rr, kl[o] * rr)) * rinv;
+                                        part[o] = fmaf(g, SS ? fmaf(-fi[o], wk, qv[u]) : qv[u], part[o]);
+                                    }
+                                }
+                            }
+                        }
+                        idx += n1;
+                    }
+#pragma unroll
+                    for (int o = 0; o < OG; o++) kahan_add(sum[o], cmp[o], part[o]);
+                }
+            }
+            if (v) {
+#pragma unroll
+                for (int o = 0; o < OG; o++)
+                    if (g0 + o < a.norb) a.out[(long)(g0 + o) * a.nt + i] = (double)sum[o] - (double)cmp[o];
             }
         }
     }
@@ -549,14 +890,15 @@ __global__ void prep_targets(const double *__restrict__ tv, const int *__restric
 // sum_j w_j (f_j - c) G + c * int G is exact for any constant c, while mixing
 // two roundings of f_i would leave delta * f_i * sum_j w_j G in the result.
 template <typename TF>
-__global__ void epilogue(const double *__restrict__ nearv, const double *__restrict__ farv,
-                         const TF *__restrict__ fsorted, const int *__restrict__ perm, int nt,
-                         const double *__restrict__ ss, double *__restrict__ out) {
+__global__ void epilogue(const double *__restrict__ nearv, const double *__restrict__ near2v,
+                         const double *__restrict__ farv, const TF *__restrict__ fsorted,
+                         const int *__restrict__ perm, int nt, const double *__restrict__ ss,
+                         double *__restrict__ out) {
     long i = (long)blockIdx.x * blockDim.x + threadIdx.x;
     int orb = blockIdx.y;
     if (i >= nt) return;
     long si = (long)orb * nt + i;
-    out[(long)orb * nt + perm[i]] = nearv[si] + farv[si] + ss[orb] * (double)fsorted[si];
+    out[(long)orb * nt + perm[i]] = (nearv[si] + near2v[si]) + farv[si] + ss[orb] * (double)fsorted[si];
 }
 
 template <typename K>
@@ -587,22 +929,24 @@ int launch_persistent(K kern, const Fields &a, int items, cudaStream_t s) {
 // ---------------------------------------------------------------------------
 template <int KERN, bool SS>
 __global__ void __launch_bounds__(FT) pair_peak_near(int reps, float *out) {
-    __shared__ float4 s_src[NTILE];
-    __shared__ float s_w[NTILE];
+    __shared__ float4 s_a[NTILE];
+    __shared__ float4 s_b[NTILE];
     for (int j = threadIdx.x; j < NTILE; j += FT) {
         float v = (float)((j * 37) % 101) * 0.01f - 0.5f;
-        s_src[j] = make_float4(v, 0.3f * v + 0.1f, 0.7f - v, 0.5f + 0.001f * j);
-        s_w[j] = 0.25f;
+        s_a[j] = make_float4(v, 0.3f * v + 0.1f, 0.7f - v, 0.5f + 0.001f * j);
+        s_b[j] = make_float4(0.f, 0.f, 0.f, 0.25f);
     }
     __syncthreads();
-    float tx[2], ty[2], tz[2], fi[2], sum[2] = {0.f, 0.f}, cmp[2] = {0.f, 0.f};
+    float tx[2], ty[2], tz[2], fi[2];
+    float sum[2] = {0.f, 0.f}, cmp[2] = {0.f, 0.f};
     for (int k = 0; k < 2; k++) {
         tx[k] = 0.01f * (threadIdx.x & 31) + 0.003f * k;
         ty[k] = 0.02f;
         tz[k] = -0.03f * (threadIdx.x >> 5);
         fi[k] = 0.3f;
     }
-    for (int r = 0; r < reps; r++) near_tile<KERN, SS, false, 2>(s_src, s_w, NTILE, tx, ty, tz, fi, sum, cmp);
+    for (int r = 0; r < reps; r++)
+        near_tile<KERN, SS, false, false, 2>(s_a, s_b, NTILE, tx, ty, tz, nullptr, 1.f, fi, sum, cmp);
     out[blockIdx.x * FT + threadIdx.x] = sum[0] + sum[1] - cmp[0] - cmp[1];
 }
 
@@ -671,13 +1015,48 @@ int launch_fields(Plan &p, const Fields &a, int precision, cudaStream_t s) {
     af.out = p.far_out;
     phase_mark(PH_NEAR, true, s);
     const bool one = p.max_batch <= FT;  // one target per thread covers every batch
+    if (precision == PREC_MIXED && KERN == KERNEL_YUKAWA && a.norb >= 4) {
+        // orbital groups share the geometry of each pair across OG orbitals
+        const bool g8 = a.norb >= 8;
+        const int gitems = p.nbatch * ((a.norb + (g8 ? 7 : 3)) / (g8 ? 8 : 4));
+        Fields a2 = an;
+        a2.out = p.near2_out;
+        if (g8) TAGI_TRY(launch_persistent(near_group<SS, 8, 0>, an, gitems, s));
+        else TAGI_TRY(launch_persistent(near_group<SS, 4, 0>, an, gitems, s));
+        phase_mark(PH_NEAR, false, s);
+        phase_mark(PH_NEAR_CLOSE, true, s);
+        if (g8) TAGI_TRY(launch_persistent(near_group<SS, 8, 1>, a2, gitems, s));
+        else TAGI_TRY(launch_persistent(near_group<SS, 4, 1>, a2, gitems, s));
+        phase_mark(PH_NEAR_CLOSE, false, s);
+        if (p.nslots == 0) return TAGI_OK;
+        phase_mark(PH_FAR, true, s);
+        if (p.n1 <= 4) {
+            if (g8) TAGI_TRY(launch_persistent(far_group<SS, 4, 8>, af, gitems, s));
+            else TAGI_TRY(launch_persistent(far_group<SS, 4, 4>, af, gitems, s));
+        } else if (p.n1 <= 8) {
+            if (g8) TAGI_TRY(launch_persistent(far_group<SS, 8, 8>, af, gitems, s));
+            else TAGI_TRY(launch_persistent(far_group<SS, 8, 4>, af, gitems, s));
+        } else {
+            if (g8) TAGI_TRY(launch_persistent(far_group<SS, MAX_DEGREE + 1, 8>, af, gitems, s));
+            else TAGI_TRY(launch_persistent(far_group<SS, MAX_DEGREE + 1, 4>, af, gitems, s));
+        }
+        phase_mark(PH_FAR, false, s);
+        return TAGI_OK;
+    }
     if (precision == PREC_MIXED) {
-        if (one) TAGI_TRY(launch_persistent(near_mixed<KERN, SS, 1>, an, items, s));
-        else TAGI_TRY(launch_persistent(near_mixed<KERN, SS, 2>, an, items, s));
+        Fields a2 = an;
+        a2.out = p.near2_out;
+        if (one) TAGI_TRY(launch_persistent(near_mixed<KERN, SS, 1, 0>, an, items, s));
+        else TAGI_TRY(launch_persistent(near_mixed<KERN, SS, 2, 0>, an, items, s));
+        phase_mark(PH_NEAR, false, s);
+        phase_mark(PH_NEAR_CLOSE, true, s);
+        if (one) TAGI_TRY(launch_persistent(near_mixed<KERN, SS, 1, 1>, a2, items, s));
+        else TAGI_TRY(launch_persistent(near_mixed<KERN, SS, 2, 1>, a2, items, s));
+        phase_mark(PH_NEAR_CLOSE, false, s);
     } else {
         TAGI_TRY(launch_persistent(near_f64<KERN, SS>, an, items, s));
+        phase_mark(PH_NEAR, false, s);
     }
-    phase_mark(PH_NEAR, false, s);
     if (p.nslots == 0) return TAGI_OK;
     phase_mark(PH_FAR, true, s);
     if (precision == PREC_MIXED) {
@@ -716,6 +1095,7 @@ int ensure_scratch(Plan &p, int norb) {
         (rc = a.alloc(&p.ft64, no * nt)) || (rc = a.alloc(&p.part, no * p.nitems * p.P)) ||
         (rc = a.alloc(&p.qhat32, no * p.nslots * p.P)) ||
         (rc = a.alloc(&p.qhat64, no * p.nslots * p.P)) || (rc = a.alloc(&p.near_out, no * nt)) ||
+        (rc = a.alloc(&p.near2_out, no * nt)) ||
         (rc = a.alloc(&p.far_out, no * nt)) || (rc = a.alloc(&p.d_kc, no)) ||
         (rc = a.alloc(&p.d_kp, no)) || (rc = a.alloc(&p.d_ss, no))) {
         p.scratch = a.ptrs;
@@ -776,9 +1156,14 @@ int convolve(Plan &p, const double *tv, const double *sv, double *out, int norb,
     a.queue = p.queue;
     a.rng_off = p.rng_off;
     a.rng = p.rng;
+    a.rng_dmin = p.rng_dmin;
     a.sx = p.src.x;
     a.sy = p.src.y;
     a.sz = p.src.z;
+    a.shi = p.src_hi;
+    a.slo = p.src_lo;
+    a.thi = p.tgt_hi;
+    a.tlo = p.tgt_lo;
     a.ns = ns;
     a.q32 = p.q32;
     a.w32 = p.sw32;
@@ -801,8 +1186,11 @@ int convolve(Plan &p, const double *tv, const double *sv, double *out, int norb,
     a.kc32 = p.d_kc;
     a.kp64 = p.d_kp;
 
-    TAGI_CUDA(cudaMemsetAsync(p.queue, 0, 2 * sizeof(int), s));
+    TAGI_CUDA(cudaMemsetAsync(p.queue, 0, 3 * sizeof(int), s));
     TAGI_CUDA(cudaMemsetAsync(p.far_out, 0, sizeof(double) * (size_t)norb * nt, s));
+    // the close-range pass writes only the targets of batches it visits; the
+    // FP64 path has a single near pass
+    TAGI_CUDA(cudaMemsetAsync(p.near2_out, 0, sizeof(double) * (size_t)norb * nt, s));
     if (kernel == KERNEL_YUKAWA) {
         if (ss) TAGI_TRY((launch_fields<KERNEL_YUKAWA, true>(p, a, precision, s)));
         else TAGI_TRY((launch_fields<KERNEL_YUKAWA, false>(p, a, precision, s)));
@@ -811,8 +1199,12 @@ int convolve(Plan &p, const double *tv, const double *sv, double *out, int norb,
         else TAGI_TRY((launch_fields<KERNEL_COULOMB, false>(p, a, precision, s)));
     }
     phase_mark(PH_GLUE, true, s);
-    if (mixed) launch(epilogue<float>, gt, 256, 0, s, p.near_out, p.far_out, p.ft32, p.tgt.perm, nt, p.d_ss, out);
-    else launch(epilogue<double>, gt, 256, 0, s, p.near_out, p.far_out, p.ft64, p.tgt.perm, nt, p.d_ss, out);
+    if (mixed)
+        launch(epilogue<float>, gt, 256, 0, s, p.near_out, p.near2_out, p.far_out, p.ft32, p.tgt.perm, nt, p.d_ss,
+               out);
+    else
+        launch(epilogue<double>, gt, 256, 0, s, p.near_out, p.near2_out, p.far_out, p.ft64, p.tgt.perm, nt, p.d_ss,
+               out);
     phase_mark(PH_GLUE, false, s);
     TAGI_LAUNCH_CHECK();
     return TAGI_OK;

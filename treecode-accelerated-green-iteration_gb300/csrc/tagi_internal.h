@@ -62,14 +62,18 @@ inline void launch(void (*kern)(KArgs...), dim3 grid, dim3 block, size_t smem, c
 }
 
 // Merged near ranges are int2 {begin, end} in sorted source order; bit 31 of
-// begin marks a range whose box touches the batch's box, where a source may
-// coincide with a target.  Always decode through these two helpers.
+// begin marks a CLOSE range: its box lies within 0.1 batch radii of the
+// batch's box (touching included).  Close ranges hold the short pairs whose
+// FP32 batch-relative coordinates would lose relative precision, and any
+// source that may coincide with a target; the field kernels give them
+// double-float coordinates and the r = 0 mask.  Decode only through these.
 __host__ __device__ __forceinline__ int range_begin(int2 r) { return r.x & 0x7fffffff; }
-__host__ __device__ __forceinline__ bool range_may_coincide(int2 r) { return r.x < 0; }
+__host__ __device__ __forceinline__ bool range_is_close(int2 r) { return r.x < 0; }
+constexpr double CLOSE_RANGE_FRACTION = 0.1;
 
 // Optional per-phase timing with CUDA events on the launching stream
 // (tagi_profile / tagi_profile_read); no-ops unless enabled.
-enum Phase { PH_TREE = 0, PH_LISTS, PH_UPWARD, PH_NEAR, PH_FAR, PH_GLUE, PH_COUNT };
+enum Phase { PH_TREE = 0, PH_LISTS, PH_UPWARD, PH_NEAR, PH_FAR, PH_GLUE, PH_NEAR_CLOSE, PH_COUNT };
 void phase_mark(int phase, bool begin, cudaStream_t s);
 
 // Stream-ordered device allocations owned by a plan (freed on destroy).
@@ -122,6 +126,7 @@ struct Plan {
     int near_total = 0, far_total = 0;
     int *rng_off = nullptr;                // merged near ranges (CSR)
     int2 *rng = nullptr;
+    float *rng_dmin = nullptr;             // lower bound of batch-to-range distance
     int rng_total = 0;
     int nslots = 0;
     int *node_slot = nullptr, *slot_node = nullptr;
@@ -130,13 +135,15 @@ struct Plan {
     int nitems = 0;
     int *item_slot = nullptr, *item_begin = nullptr, *item_end = nullptr;
     int *slot_item_off = nullptr;          // [nslots+1]
+    float4 *src_hi = nullptr, *src_lo = nullptr;  // FP32 hi/lo of sorted source x, y, z
+    float4 *tgt_hi = nullptr, *tgt_lo = nullptr;  // same for targets
     double *sw64 = nullptr;                // sorted source weights
     float *sw32 = nullptr;
     float *what32 = nullptr;               // weight modified charges [slot][P]
     double *what64 = nullptr;              // FP64 set, built on first FP64 use
     bool what64_ready = false;
     int *order_near = nullptr, *order_far = nullptr;   // batches, heaviest first
-    int *queue = nullptr;                  // work-queue counters (2 ints)
+    int *queue = nullptr;                  // work-queue counters (3 ints)
     int *err_flag = nullptr;
     double cheb[MAX_DEGREE + 1];           // cos(m pi / degree)
     // per-convolution scratch (grown on demand)
@@ -150,6 +157,7 @@ struct Plan {
     float *qhat32 = nullptr;               // [norb][nslots][P]
     double *qhat64 = nullptr;
     double *near_out = nullptr, *far_out = nullptr;  // [norb][nt] sorted order
+    double *near2_out = nullptr;           // close-range pass of the near field
     float *d_kc = nullptr;                 // [norb] exp2 constants
     double *d_kp = nullptr, *d_ss = nullptr;         // [norb] k (or a), SS factor
     std::vector<float> h_kc;
@@ -157,6 +165,7 @@ struct Plan {
     std::vector<void *> scratch;           // freed on regrow / destroy
     // statistics (host)
     double near_pairs = 0, far_pairs = 0;  // pair interactions per orbital
+    double near_close_pairs = 0;           // part of near_pairs in close ranges
 };
 
 // scan_sort.cu

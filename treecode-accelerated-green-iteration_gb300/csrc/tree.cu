@@ -446,69 +446,76 @@ __global__ void assign_slots(int nn, const int *__restrict__ flag, const int *__
     }
 }
 
-// Merge consecutive near entries whose source ranges touch.  A merged range
-// whose bounding box touches the batch's box (closed boxes, with a relative
-// margin) may hold a source that coincides with a target: its begin index is
-// stored with bit 31 set, and the field kernels mask r = 0 pairs only there.
-__device__ __forceinline__ bool boxes_touch(const double *cb, const double *hb, const double *lo,
-                                            const double *hi) {
+// Gap between the batch box (center cb, half widths hb) and a node box: the
+// Euclidean distance between the closed boxes, reduced by a relative margin so
+// that touching boxes give 0.
+__device__ __forceinline__ double box_gap(const double *cb, const double *hb, const double *cc,
+                                          const double *hc) {
+    double g2 = 0.0;
 #pragma unroll
     for (int d = 0; d < 3; d++) {
-        double c = 0.5 * (lo[d] + hi[d]), h = 0.5 * (hi[d] - lo[d]);
-        double gap = fabs(cb[d] - c) - (hb[d] + h);
-        double tol = 1e-12 * (fabs(cb[d]) + fabs(c) + hb[d] + h) + 1e-300;
-        if (gap > tol) return false;
+        double gap = fabs(cb[d] - cc[d]) - (hb[d] + hc[d]);
+        gap -= 1e-12 * (fabs(cb[d]) + fabs(cc[d]) + hb[d] + hc[d]) + 1e-300;
+        if (gap > 0.0) g2 += gap * gap;
     }
-    return true;
+    return sqrt(g2);
 }
 
+// Merge consecutive near entries whose source ranges touch and whose nodes
+// are of the same class: a node is CLOSE when its box lies within
+// CLOSE_RANGE_FRACTION batch radii of the batch's box (touching included).
+// Close ranges are stored with bit 31 of their begin set (range_is_close).
+// rng_dmin = smallest node gap of the range, rounded down: a lower bound of
+// every pair distance in it.
 template <bool FILL>
 __global__ void merge_ranges(int nbatch, const int *__restrict__ near_off,
                              const int *__restrict__ near_list, const int *__restrict__ sbegin,
                              const int *__restrict__ send, const double *__restrict__ scenter,
                              const double *__restrict__ shalf, const int *__restrict__ batch_node,
                              const double *__restrict__ tcenter, const double *__restrict__ thalf,
+                             const double *__restrict__ tradius,
                              int *__restrict__ cnt, const int *__restrict__ rng_off,
-                             int2 *__restrict__ rng) {
+                             int2 *__restrict__ rng, float *__restrict__ rng_dmin) {
     int b = blockIdx.x * blockDim.x + threadIdx.x;
     if (b >= nbatch) return;
     const int bn = batch_node[b];
     const double cb[3] = {tcenter[3L * bn], tcenter[3L * bn + 1], tcenter[3L * bn + 2]};
     const double hb[3] = {thalf[3L * bn], thalf[3L * bn + 1], thalf[3L * bn + 2]};
+    const double close_gap = CLOSE_RANGE_FRACTION * tradius[bn];
     int k = 0;
     int cb0 = -1, ce = -1;
-    double lo[3], hi[3];
+    bool cclose = false;
+    double cmin = INFINITY;
     for (int e = near_off[b]; e <= near_off[b + 1]; e++) {
         int c = -1, nb = -1, ne = -1;
+        bool nclose = false;
+        double gap = 0.0;
         if (e < near_off[b + 1]) {
             c = near_list[e];
             nb = sbegin[c];
             ne = send[c];
+            const double cc[3] = {scenter[3L * c], scenter[3L * c + 1], scenter[3L * c + 2]};
+            const double hc[3] = {shalf[3L * c], shalf[3L * c + 1], shalf[3L * c + 2]};
+            gap = box_gap(cb, hb, cc, hc);
+            nclose = gap <= close_gap;
         }
-        if (c >= 0 && cb0 >= 0 && nb == ce) {
+        if (c >= 0 && cb0 >= 0 && nb == ce && nclose == cclose) {
             ce = ne;
-        } else {
-            if (cb0 >= 0) {
-                if (FILL) {
-                    int flag = boxes_touch(cb, hb, lo, hi) ? (int)0x80000000u : 0;
-                    rng[rng_off[b] + k] = make_int2(cb0 | flag, ce);
-                }
-                k++;
-            }
-            if (c < 0) break;
-            cb0 = nb;
-            ce = ne;
-#pragma unroll
-            for (int d = 0; d < 3; d++) {
-                lo[d] = INFINITY;
-                hi[d] = -INFINITY;
-            }
+            cmin = fmin(cmin, gap);
+            continue;
         }
-#pragma unroll
-        for (int d = 0; d < 3; d++) {
-            lo[d] = fmin(lo[d], scenter[3L * c + d] - shalf[3L * c + d]);
-            hi[d] = fmax(hi[d], scenter[3L * c + d] + shalf[3L * c + d]);
+        if (cb0 >= 0) {
+            if (FILL) {
+                rng[rng_off[b] + k] = make_int2(cb0 | (cclose ? (int)0x80000000u : 0), ce);
+                rng_dmin[rng_off[b] + k] = (float)(cmin * (1.0 - 1e-6));
+            }
+            k++;
         }
+        if (c < 0) break;
+        cb0 = nb;
+        ce = ne;
+        cclose = nclose;
+        cmin = gap;
     }
     if (!FILL) cnt[b] = k;
 }
@@ -517,14 +524,20 @@ __global__ void batch_costs(int nbatch, const int *__restrict__ batch_node,
                             const int *__restrict__ tbegin, const int *__restrict__ tend,
                             const int *__restrict__ rng_off, const int2 *__restrict__ rng,
                             const int *__restrict__ far_off, long long *__restrict__ cost_near,
-                            long long *__restrict__ cost_far, int *__restrict__ bsize) {
+                            long long *__restrict__ cost_far, int *__restrict__ bsize,
+                            long long *__restrict__ cost_close) {
     int b = blockIdx.x * blockDim.x + threadIdx.x;
     if (b >= nbatch) return;
     int bn = batch_node[b];
     long long nb = tend[bn] - tbegin[bn];
-    long long s = 0;
-    for (int e = rng_off[b]; e < rng_off[b + 1]; e++) s += rng[e].y - range_begin(rng[e]);
+    long long s = 0, sc = 0;
+    for (int e = rng_off[b]; e < rng_off[b + 1]; e++) {
+        const long long len = rng[e].y - range_begin(rng[e]);
+        s += len;
+        if (range_is_close(rng[e])) sc += len;
+    }
     cost_near[b] = nb * s;
+    cost_close[b] = nb * sc;
     cost_far[b] = nb * (long long)(far_off[b + 1] - far_off[b]);
     bsize[b] = (int)nb;
 }
@@ -663,14 +676,14 @@ int build_lists(Plan &p, cudaStream_t s) {
         if ((rc = tmp.alloc(&rcnt, nb))) break;
         if ((rc = ar.alloc(&p.rng_off, nb + 1))) break;
         launch(merge_ranges<false>, (nb + 127) / 128, 128, 0, s, nb, p.near_off, p.near_list, p.src.begin,
-               p.src.end, p.src.center, p.src.half, p.batch_node, p.tgt.center, p.tgt.half, rcnt,
-               nullptr, nullptr);
+               p.src.end, p.src.center, p.src.half, p.batch_node, p.tgt.center, p.tgt.half, p.tgt.radius, rcnt,
+               nullptr, nullptr, nullptr);
         if ((rc = exclusive_scan(rcnt, p.rng_off, nb, p.rng_off + nb, tmp, s))) break;
         if ((rc = sync_int(p.rng_off + nb, &p.rng_total))) break;
-        if ((rc = ar.alloc(&p.rng, p.rng_total))) break;
+        if ((rc = ar.alloc(&p.rng, p.rng_total)) || (rc = ar.alloc(&p.rng_dmin, p.rng_total))) break;
         launch(merge_ranges<true>, (nb + 127) / 128, 128, 0, s, nb, p.near_off, p.near_list, p.src.begin,
-               p.src.end, p.src.center, p.src.half, p.batch_node, p.tgt.center, p.tgt.half, nullptr,
-               p.rng_off, p.rng);
+               p.src.end, p.src.center, p.src.half, p.batch_node, p.tgt.center, p.tgt.half, p.tgt.radius, nullptr,
+               p.rng_off, p.rng, p.rng_dmin);
 
         // Upward-pass work items.
         if ((rc = ar.alloc(&p.slot_item_off, p.nslots + 1))) break;
@@ -695,25 +708,30 @@ int build_lists(Plan &p, cudaStream_t s) {
                                                               p.item_slot, p.item_begin, p.item_end);
 
         // Work order for the field kernels: heaviest batch first.
-        long long *cn = nullptr, *cf = nullptr;
+        long long *cn = nullptr, *cf = nullptr, *cc2 = nullptr;
         int *bsz = nullptr;
-        if ((rc = tmp.alloc(&cn, nb)) || (rc = tmp.alloc(&cf, nb)) || (rc = tmp.alloc(&bsz, nb))) break;
+        if ((rc = tmp.alloc(&cn, nb)) || (rc = tmp.alloc(&cf, nb)) || (rc = tmp.alloc(&bsz, nb)) ||
+            (rc = tmp.alloc(&cc2, nb)))
+            break;
         launch(batch_costs, (nb + 127) / 128, 128, 0, s, nb, p.batch_node, p.tgt.begin, p.tgt.end,
-                                                     p.rng_off, p.rng, p.far_off, cn, cf, bsz);
-        std::vector<long long> hcn(nb), hcf(nb);
+                                                     p.rng_off, p.rng, p.far_off, cn, cf, bsz, cc2);
+        std::vector<long long> hcn(nb), hcf(nb), hcc(nb);
         std::vector<int> hsz(nb);
         if (cudaMemcpyAsync(hcn.data(), cn, sizeof(long long) * nb, cudaMemcpyDeviceToHost, s) ||
             cudaMemcpyAsync(hcf.data(), cf, sizeof(long long) * nb, cudaMemcpyDeviceToHost, s) ||
             cudaMemcpyAsync(hsz.data(), bsz, sizeof(int) * nb, cudaMemcpyDeviceToHost, s) ||
+            cudaMemcpyAsync(hcc.data(), cc2, sizeof(long long) * nb, cudaMemcpyDeviceToHost, s) ||
             cudaStreamSynchronize(s)) {
             rc = set_error(TAGI_ERR_CUDA, "batch cost copy failed");
             break;
         }
         p.near_pairs = 0;
+        p.near_close_pairs = 0;
         p.far_pairs = 0;
         p.max_batch = 0;
         for (int b = 0; b < nb; b++) {
             p.near_pairs += (double)hcn[b];
+            p.near_close_pairs += (double)hcc[b];
             p.far_pairs += (double)hcf[b] * p.P;
             p.max_batch = std::max(p.max_batch, hsz[b]);
         }

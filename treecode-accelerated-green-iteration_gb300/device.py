@@ -105,10 +105,11 @@ class TreecodePlan:
         return out[0] if squeeze else out
 
     def info(self):
-        v = np.zeros(12)
+        v = np.zeros(13)
         _native.check(_native.lib().tagi_plan_info(self._h, _native.dptr(v)))
         keys = ("src_nodes", "tgt_nodes", "batches", "near_entries", "far_entries", "slots", "P",
-                "upward_items", "near_ranges", "max_batch", "near_pairs", "far_pairs")
+                "upward_items", "near_ranges", "max_batch", "near_pairs", "far_pairs",
+                "near_close_pairs")
         return {k: (float(x) if k.endswith("pairs") else int(x)) for k, x in zip(keys, v)}
 
     def tree(self, which):
