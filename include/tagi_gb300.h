@@ -39,7 +39,8 @@ enum {
     TAGI_ERR_ARG = 1,
     TAGI_ERR_CUDA = 2,
     TAGI_ERR_UNSUPPORTED = 3,
-    TAGI_ERR_DEVICE = 4
+    TAGI_ERR_DEVICE = 4,
+    TAGI_ERR_STATE = 5  /* call order: e.g. a capture before the first uncaptured call */
 };
 enum { TAGI_PREC_MIXED = 0, TAGI_PREC_FP64 = 1 };
 
@@ -131,6 +132,72 @@ int tagi_plan_convolve(tagi_plan *plan, int numOrbitals, const double *targetVal
                        const double *sourceValues, double *output, int kernel,
                        int numberOfKernelParameters, const double *kernelParameters,
                        int singularity, int precision, void *stream);
+
+/* tagi_plan_convolve with two more controls.  kernelParametersOnDevice != 0:
+ * kernelParameters is a DEVICE array (same layout), read when the call runs
+ * on the GPU -- the form for calls inside a captured graph, whose parameters
+ * (k_i = sqrt(-2 eps_i)) change between replays; such values are not checked
+ * on the host: an unusable one (not finite, or <= 0 where the kernel uses it)
+ * gives NaN output and sets a flag that tagi_plan_check_parameters returns.
+ * orbitalsPerItem: 0 = automatic, 1, 4 or 8 (Yukawa mixed precision shares
+ * each pair's geometry across a group of orbitals; other cases use 1).
+ * Extends callTreedriver (BaryTreeInterface.py:88-158), which has neither. */
+int tagi_plan_convolve_ex(tagi_plan *plan, int numOrbitals, const double *targetValues,
+                          const double *sourceValues, double *output, int kernel,
+                          int numberOfKernelParameters, const double *kernelParameters,
+                          int kernelParametersOnDevice, int singularity, int precision,
+                          int orbitalsPerItem, void *stream);
+/* Waits for the stream, returns (and clears) the plan's flag of unusable
+ * device kernel parameters: *flags != 0 if any call since the last check
+ * had one. */
+int tagi_plan_check_parameters(tagi_plan *plan, int *flags, void *stream);
+
+/* Several systems (plans over different meshes, each with its own orbital
+ * count) convolved together: per-system charge preparation and upward pass,
+ * then ONE persistent launch per field pass (near, near close ranges, far)
+ * whose work list holds every (system, target batch, orbital group) item,
+ * heaviest first.  Up to 8 systems; all share kernel and precision.  Plans
+ * are borrowed and must outlive the object.  No counterpart in the reference
+ * (one BaryTreeInterface call per orbital, greenIterationFixedPoint.py:314). */
+typedef struct tagi_systems tagi_systems;
+int tagi_systems_create(tagi_systems **systems, int numSystems, tagi_plan *const *plans,
+                        const int *numOrbitals, int kernel, int precision, int orbitalsPerItem,
+                        void *stream);
+/* Arrays of numSystems device pointers, each laid out as tagi_plan_convolve's
+ * arguments for that system; kernelParameters[i] host or device (flag). */
+int tagi_systems_convolve(tagi_systems *systems, const double *const *targetValues,
+                          const double *const *sourceValues, double *const *outputs,
+                          int numberOfKernelParameters, const double *const *kernelParameters,
+                          int kernelParametersOnDevice, int singularity, void *stream);
+/* info[0..4] = systems, orbitals per item, work items of the near pass, the
+ * close-range pass and the far pass. */
+int tagi_systems_info(const tagi_systems *systems, int *info);
+int tagi_systems_destroy(tagi_systems *systems);
+
+/* One-shot batched convolution over numSystems meshes concatenated in device
+ * arrays x, y, z, w (system s = points pointOffsets[s] .. pointOffsets[s+1]-1,
+ * targets = sources as in Green iteration).  values/output hold, system after
+ * system, numOrbitals[s] rows of that system's point count.  kernelParameters
+ * (HOST): one value per orbital, system after system.  Systems go 8 per
+ * launch. */
+int tagi_treecode_batched(int numSystems, const int *pointOffsets, const int *numOrbitals,
+                          const double *x, const double *y, const double *z, const double *w,
+                          const double *values, double *output, int kernel,
+                          const double *kernelParameters, int singularity, double theta,
+                          int degree, int sourceLeafSize, int targetLeafSize, double sizeCheck,
+                          int precision, void *stream);
+
+/* CUDA-graph capture of a call sequence on a created (non-default) stream:
+ * begin, then any of this library's device calls (each made once uncaptured
+ * before, so nothing allocates; kernel parameters on the device), then end.
+ * Replays re-run the captured launches on the data then in the same
+ * buffers. */
+typedef struct tagi_graph tagi_graph;
+int tagi_graph_begin(void *stream);
+int tagi_graph_end(void *stream, tagi_graph **graph);
+int tagi_graph_launch(tagi_graph *graph, void *stream);
+int tagi_graph_nodes(const tagi_graph *graph, int *numNodes);
+int tagi_graph_destroy(tagi_graph *graph);
 
 /* Plan statistics: info[0..12] = source nodes, target nodes, batches,
  * near-list entries, far-list entries, slots, proxy points P, upward items,

@@ -16,7 +16,7 @@ _vp = ctypes.c_void_p
 _i = ctypes.c_int
 _d = ctypes.c_double
 
-TAGI_OK, TAGI_ERR_ARG, TAGI_ERR_CUDA, TAGI_ERR_UNSUPPORTED, TAGI_ERR_DEVICE = range(5)
+TAGI_OK, TAGI_ERR_ARG, TAGI_ERR_CUDA, TAGI_ERR_UNSUPPORTED, TAGI_ERR_DEVICE, TAGI_ERR_STATE = range(6)
 PREC_MIXED, PREC_FP64 = 0, 1
 
 _treecode_params = [_i, _i, _dp, _dp, _dp, _dp, _dp, _dp, _dp, _dp, _dp, _dp, _i, _i, _dp, _i, _i, _i,
@@ -34,6 +34,20 @@ SIGNATURES = {
                               _i, _i, _d, _vp]),
     "tagi_plan_destroy": (_i, [_vp]),
     "tagi_plan_convolve": (_i, [_vp, _i, _vp, _vp, _vp, _i, _i, _dp, _i, _i, _vp]),
+    "tagi_plan_convolve_ex": (_i, [_vp, _i, _vp, _vp, _vp, _i, _i, _vp, _i, _i, _i, _i, _vp]),
+    "tagi_plan_check_parameters": (_i, [_vp, _ip, _vp]),
+    "tagi_systems_create": (_i, [ctypes.POINTER(_vp), _i, ctypes.POINTER(_vp), _ip, _i, _i, _i, _vp]),
+    "tagi_systems_convolve": (_i, [_vp, ctypes.POINTER(_vp), ctypes.POINTER(_vp), ctypes.POINTER(_vp), _i,
+                                   ctypes.POINTER(_vp), _i, _i, _vp]),
+    "tagi_systems_info": (_i, [_vp, _ip]),
+    "tagi_systems_destroy": (_i, [_vp]),
+    "tagi_treecode_batched": (_i, [_i, _ip, _ip, _vp, _vp, _vp, _vp, _vp, _vp, _i, _dp, _i, _d, _i, _i, _i,
+                                   _d, _i, _vp]),
+    "tagi_graph_begin": (_i, [_vp]),
+    "tagi_graph_end": (_i, [_vp, ctypes.POINTER(_vp)]),
+    "tagi_graph_launch": (_i, [_vp, _vp]),
+    "tagi_graph_nodes": (_i, [_vp, _ip]),
+    "tagi_graph_destroy": (_i, [_vp]),
     "tagi_plan_info": (_i, [_vp, _dp]),
     "tagi_plan_get_tree": (_i, [_vp, _i, _u64p, _ip, _ip, _ip, _ip, _ip, _ip, _dp, _dp, _dp]),
     "tagi_plan_get_lists": (_i, [_vp, _ip, _ip, _ip, _ip, _ip, _ip]),

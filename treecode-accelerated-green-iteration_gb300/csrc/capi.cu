@@ -49,24 +49,6 @@ int set_error(int code, const char *fmt, ...) {
 
 int last_error() { return g_err; }
 
-namespace {
-
-int default_precision() {
-    if (g_precision < 0) {
-        const char *e = getenv("TAGI_PRECISION");
-        g_precision = (e && (strcmp(e, "mixed") == 0 || strcmp(e, "MIXED") == 0)) ? PREC_MIXED : PREC_FP64;
-    }
-    return g_precision;
-}
-
-void beta_map(double beta, double *theta, int *degree, int *sl, int *tl) {
-    double b = beta < 0 ? 0 : (beta > 1 ? 1 : beta);
-    *degree = std::min(MAX_DEGREE, std::max(1, (int)std::lround(1.0 + 9.0 * b)));
-    *theta = 0.95 - 0.6 * b;
-    *sl = 500;
-    *tl = 500;
-}
-
 int validate(int nt, int ns, int kernel, int nkp, const double *kp, int sing, int approx,
              int ctype, double theta, int degree, int sl, int tl, double size_check, int precision) {
     if (nt < 0 || ns < 0) return set_error(TAGI_ERR_ARG, "negative point count (%d targets, %d sources)", nt, ns);
@@ -96,6 +78,24 @@ int validate_kparam(int kernel, int sing, double k) {
     if (kernel == KERNEL_COULOMB && sing == SING_SUBTRACTION && !(k > 0.0))
         return set_error(TAGI_ERR_ARG, "Coulomb subtraction parameter alpha = %g must be > 0", k);
     return TAGI_OK;
+}
+
+namespace {
+
+int default_precision() {
+    if (g_precision < 0) {
+        const char *e = getenv("TAGI_PRECISION");
+        g_precision = (e && (strcmp(e, "mixed") == 0 || strcmp(e, "MIXED") == 0)) ? PREC_MIXED : PREC_FP64;
+    }
+    return g_precision;
+}
+
+void beta_map(double beta, double *theta, int *degree, int *sl, int *tl) {
+    double b = beta < 0 ? 0 : (beta > 1 ? 1 : beta);
+    *degree = std::min(MAX_DEGREE, std::max(1, (int)std::lround(1.0 + 9.0 * b)));
+    *theta = 0.95 - 0.6 * b;
+    *sl = 500;
+    *tl = 500;
 }
 
 __global__ void gather_weights(const double *__restrict__ w, const int *__restrict__ perm, int n,
@@ -161,8 +161,9 @@ int plan_create(Plan **out, int nt, const double *tx, const double *ty, const do
     for (int m = 0; m <= MAX_DEGREE; m++) p->cheb[m] = m <= degree ? std::cos(M_PI * (double)m / (double)degree) : 0.0;
     int rc = TAGI_OK;
     do {
-        if ((rc = p->arena.alloc(&p->queue, 3)) || (rc = p->arena.alloc(&p->err_flag, 1))) break;
-        cudaMemsetAsync(p->err_flag, 0, sizeof(int), s);
+        // err_flag[0]: tree/list build; err_flag[1]: kernel parameters a call could not use
+        if ((rc = p->arena.alloc(&p->queue, 3)) || (rc = p->arena.alloc(&p->err_flag, 2))) break;
+        cudaMemsetAsync(p->err_flag, 0, 2 * sizeof(int), s);
         phase_mark(PH_TREE, true, s);
         if ((rc = build_tree(p->src, sx, sy, sz, ns, sl, p->arena, p->err_flag, s))) break;
         if ((rc = build_tree(p->tgt, tx, ty, tz, nt, tl, p->arena, p->err_flag, s))) break;
@@ -196,6 +197,7 @@ void plan_destroy(Plan *p) {
     if (!p) return;
     cudaDeviceSynchronize();
     for (void *v : p->scratch) cudaFree(v);
+    for (Schedule &sc : p->scheds) sc.release();
     for (void *v : p->arena.ptrs) cudaFree(v);
     delete p;
 }

@@ -31,7 +31,9 @@
 // replaced by (proxy point s_k, qhat_k, what_k).
 #include "tagi_internal.h"
 
+#include <algorithm>
 #include <cmath>
+#include <type_traits>
 
 namespace tagi {
 
@@ -58,9 +60,7 @@ struct Fields {
     const int *tbegin, *tend;
     const double *tcenter, *tradius;
     const int *batch_node;
-    const int *order;
     int nbatch, nt, norb;
-    int *queue;
     // near side
     const int *rng_off;
     const int2 *rng;
@@ -80,17 +80,22 @@ struct Fields {
     // per orbital
     const float *ft32;            // [norb][nt] sorted target values
     const double *ft64;
-    const float *kc32;            // [norb] coordinate scale sc (see coordinate_scale)
+    const float *kc32;            // [norb] coordinate scale sc (orbital_constants)
     const double *kp64;           // [norb] kernel parameter k or a
     double *out;                  // [norb][nt] sorted order
 };
 
-// Coordinate scale sc of an orbital (see the header comment).
-inline float coordinate_scale(int kernel, int singularity, double kp) {
-    if (kernel == KERNEL_YUKAWA) return (float)(kp * LOG2E);
-    if (singularity == SING_SUBTRACTION) return (float)(kp * std::sqrt(LOG2E));
-    return 1.0f;
-}
+// Argument of every persistent field kernel: the work list of this pass and
+// up to MAX_SYSTEMS systems' fields.  It is a __grid_constant__ parameter, so
+// a CTA reads the fields of its current item's system straight from the
+// parameter bank (dynamic index, no local copy).
+struct Work {
+    const int2 *items;            // {batch, sys << 16 | first orbital}, heaviest first
+    int nitems;
+    int *queue;                   // this pass's work counter
+    Fields sys[MAX_SYSTEMS];
+};
+static_assert(sizeof(Work) <= 4096, "field-kernel parameter block above 4 KB");
 
 __device__ __forceinline__ int next_item(int *queue, int *s_item) {
     __syncthreads();
@@ -218,19 +223,19 @@ __device__ __forceinline__ void split_f32(double v, float &hi, float &lo) {
 #define TAGI_NEAR_MINB 3   // resident CTAs per SM the near kernel is compiled for
 #endif
 template <int KERN, bool SS, int NT, int PASS>
-__global__ void __launch_bounds__(FT, TAGI_NEAR_MINB) near_mixed(Fields a) {
+__global__ void __launch_bounds__(FT, TAGI_NEAR_MINB) near_mixed(const __grid_constant__ Work w) {
     __shared__ float4 s_a[NTILE];
     __shared__ float4 s_b[NTILE];
     __shared__ float s_tlo[FT * NT * 3];
     __shared__ int s_item;
     const int tid = threadIdx.x;
-    const int total = a.nbatch * a.norb;
     float *my_tl = s_tlo + 3 * NT * tid;
     for (;;) {
-        const int item = next_item(a.queue + (PASS == 1 ? 2 : 0), &s_item);
-        if (item >= total) break;
-        const int b = a.order[item / a.norb];
-        const int orb = item - (item / a.norb) * a.norb;
+        const int item = next_item(w.queue, &s_item);
+        if (item >= w.nitems) break;
+        const int2 it = w.items[item];
+        const Fields &a = w.sys[it.y >> 16];
+        const int b = it.x, orb = it.y & 0xffff;
         const int bn = a.batch_node[b];
         const int tb = a.tbegin[bn], te = a.tend[bn];
         const double cbx = a.tcenter[3L * bn], cby = a.tcenter[3L * bn + 1],
@@ -387,19 +392,19 @@ __device__ __forceinline__ void far_cluster(const float2 *__restrict__ s_qw, con
 }
 
 template <int KERN, bool SS, int MAXN1, int NT>
-__global__ void __launch_bounds__(FT, 2) far_mixed(Fields a) {
+__global__ void __launch_bounds__(FT, 2) far_mixed(const __grid_constant__ Work w) {
     constexpr int MAXP = MAXN1 * MAXN1 * MAXN1;
     __shared__ float2 s_qw[MAXP];
     __shared__ float s_p[3][MAXN1];
     __shared__ int s_item, s_mode;
     const int tid = threadIdx.x;
-    const int n1 = a.n1, P = a.P;
-    const int total = a.nbatch * a.norb;
     for (;;) {
-        const int item = next_item(a.queue + 1, &s_item);
-        if (item >= total) break;
-        const int b = a.order[item / a.norb];
-        const int orb = item - (item / a.norb) * a.norb;
+        const int item = next_item(w.queue, &s_item);
+        if (item >= w.nitems) break;
+        const int2 it = w.items[item];
+        const Fields &a = w.sys[it.y >> 16];
+        const int b = it.x, orb = it.y & 0xffff;
+        const int n1 = a.n1, P = a.P;
         const int f0 = a.far_off[b], f1 = a.far_off[b + 1];
         if (f0 == f1) continue;
         const int bn = a.batch_node[b];
@@ -517,19 +522,18 @@ __device__ __forceinline__ void group_tile(const float4 *__restrict__ s_xyzw, co
 }
 
 template <bool SS, int OG, int PASS>
-__global__ void __launch_bounds__(FT, 2) near_group(Fields a) {
+__global__ void __launch_bounds__(FT, 2) near_group(const __grid_constant__ Work w) {
     __shared__ float4 s_xyzw[GTILE];
     __shared__ float4 s_lo[GTILE];
     __shared__ float4 s_q4[GTILE * OG / 4];
     __shared__ int s_item;
     const int tid = threadIdx.x;
-    const int ngroups = (a.norb + OG - 1) / OG;
-    const int total = a.nbatch * ngroups;
     for (;;) {
-        const int item = next_item(a.queue + (PASS == 1 ? 2 : 0), &s_item);
-        if (item >= total) break;
-        const int b = a.order[item / ngroups];
-        const int g0 = (item - (item / ngroups) * ngroups) * OG;
+        const int item = next_item(w.queue, &s_item);
+        if (item >= w.nitems) break;
+        const int2 it = w.items[item];
+        const Fields &a = w.sys[it.y >> 16];
+        const int b = it.x, g0 = it.y & 0xffff;
         const int bn = a.batch_node[b];
         const int tb = a.tbegin[bn], te = a.tend[bn];
         const double cbx = a.tcenter[3L * bn], cby = a.tcenter[3L * bn + 1], cbz = a.tcenter[3L * bn + 2];
@@ -617,21 +621,20 @@ __global__ void __launch_bounds__(FT, 2) near_group(Fields a) {
 }
 
 template <bool SS, int MAXN1, int OG>
-__global__ void __launch_bounds__(FT, 2) far_group(Fields a) {
+__global__ void __launch_bounds__(FT, 2) far_group(const __grid_constant__ Work w) {
     constexpr int MAXP = MAXN1 * MAXN1 * MAXN1;
     __shared__ float4 s_q4[MAXP * OG / 4];
     __shared__ float s_w[MAXP];
     __shared__ float s_p[3][MAXN1];
     __shared__ int s_item;
     const int tid = threadIdx.x;
-    const int n1 = a.n1, P = a.P;
-    const int ngroups = (a.norb + OG - 1) / OG;
-    const int total = a.nbatch * ngroups;
     for (;;) {
-        const int item = next_item(a.queue + 1, &s_item);
-        if (item >= total) break;
-        const int b = a.order[item / ngroups];
-        const int g0 = (item - (item / ngroups) * ngroups) * OG;
+        const int item = next_item(w.queue, &s_item);
+        if (item >= w.nitems) break;
+        const int2 it = w.items[item];
+        const Fields &a = w.sys[it.y >> 16];
+        const int b = it.x, g0 = it.y & 0xffff;
+        const int n1 = a.n1, P = a.P;
         const int f0 = a.far_off[b], f1 = a.far_off[b + 1];
         if (f0 == f1) continue;
         const int bn = a.batch_node[b];
@@ -743,17 +746,17 @@ __device__ __forceinline__ double pair_f64(double dx, double dy, double dz, doub
 }
 
 template <int KERN, bool SS>
-__global__ void __launch_bounds__(FT) near_f64(Fields a) {
+__global__ void __launch_bounds__(FT) near_f64(const __grid_constant__ Work w) {
     constexpr int T64 = 256;
     __shared__ double s_x[T64], s_y[T64], s_z[T64], s_f[T64], s_w[T64];
     __shared__ int s_item;
     const int tid = threadIdx.x;
-    const int total = a.nbatch * a.norb;
     for (;;) {
-        const int item = next_item(a.queue, &s_item);
-        if (item >= total) break;
-        const int b = a.order[item / a.norb];
-        const int orb = item - (item / a.norb) * a.norb;
+        const int item = next_item(w.queue, &s_item);
+        if (item >= w.nitems) break;
+        const int2 it = w.items[item];
+        const Fields &a = w.sys[it.y >> 16];
+        const int b = it.x, orb = it.y & 0xffff;
         const int bn = a.batch_node[b];
         const int tb = a.tbegin[bn], te = a.tend[bn];
         const double kp = a.kp64[orb];
@@ -791,19 +794,19 @@ __global__ void __launch_bounds__(FT) near_f64(Fields a) {
 }
 
 template <int KERN, bool SS, int MAXN1>
-__global__ void __launch_bounds__(FT) far_f64(Fields a) {
+__global__ void __launch_bounds__(FT) far_f64(const __grid_constant__ Work w) {
     constexpr int MAXP = MAXN1 * MAXN1 * MAXN1;
     __shared__ double s_q[MAXP], s_wh[MAXP];
     __shared__ double s_p[3][MAXN1];
     __shared__ int s_item;
     const int tid = threadIdx.x;
-    const int n1 = a.n1, P = a.P;
-    const int total = a.nbatch * a.norb;
     for (;;) {
-        const int item = next_item(a.queue + 1, &s_item);
-        if (item >= total) break;
-        const int b = a.order[item / a.norb];
-        const int orb = item - (item / a.norb) * a.norb;
+        const int item = next_item(w.queue, &s_item);
+        if (item >= w.nitems) break;
+        const int2 it = w.items[item];
+        const Fields &a = w.sys[it.y >> 16];
+        const int b = it.x, orb = it.y & 0xffff;
+        const int n1 = a.n1, P = a.P;
         const int f0 = a.far_off[b], f1 = a.far_off[b + 1];
         if (f0 == f1) continue;
         const int bn = a.batch_node[b];
@@ -912,12 +915,13 @@ int occupancy_grid(K kern, int *grid) {
 }
 
 template <typename K>
-int launch_persistent(K kern, const Fields &a, int items, cudaStream_t s) {
+int launch_persistent(K kern, const Work &w, cudaStream_t s) {
+    if (w.nitems == 0) return TAGI_OK;
     int grid = 0;
     TAGI_TRY(occupancy_grid(kern, &grid));
-    if (grid > items) grid = items;
+    if (grid > w.nitems) grid = w.nitems;
     if (grid < 1) grid = 1;
-    launch(kern, grid, FT, 0, s, a);
+    launch(kern, grid, FT, 0, s, w);
     TAGI_LAUNCH_CHECK();
     return TAGI_OK;
 }
@@ -1005,142 +1009,117 @@ int run_pair_peak(int variant, double *pairs_per_s, cudaStream_t s) {
     return TAGI_OK;
 }
 
+// Kernel shape shared by every system of one field launch.
+struct LaunchShape {
+    int og = 1;     // orbitals per item (orbital-group kernels) or 1
+    int nt = 1;     // targets per thread: 2 when some batch holds more than FT targets
+    int maxn1 = 1;  // largest proxy-grid edge n + 1
+};
+
 template <int KERN, bool SS>
-int launch_fields(Plan &p, const Fields &a, int precision, cudaStream_t s) {
-    const int items = p.nbatch * a.norb;
-    Fields an = a, af = a;
-    an.order = p.order_near;
-    an.out = p.near_out;
-    af.order = p.order_far;
-    af.out = p.far_out;
+int launch_fields(const SysCall *calls, const Fields *f, int nsys, const Schedule &sc, const LaunchShape &sh,
+                  int precision, int *queue, cudaStream_t s) {
+    Work wn{};
+    wn.queue = queue;
+    for (int i = 0; i < nsys; i++) wn.sys[i] = f[i];
+    Work wc = wn, wf = wn;
+    for (int i = 0; i < nsys; i++) {
+        wn.sys[i].out = calls[i].p->near_out;
+        wc.sys[i].out = calls[i].p->near2_out;
+        wf.sys[i].out = calls[i].p->far_out;
+    }
+    wn.items = sc.items + sc.off[0];
+    wn.nitems = sc.count[0];
+    wc.items = sc.items + sc.off[1];
+    wc.nitems = sc.count[1];
+    wc.queue = queue + 2;
+    wf.items = sc.items + sc.off[2];
+    wf.nitems = sc.count[2];
+    wf.queue = queue + 1;
+    const bool one = sh.nt == 1;
     phase_mark(PH_NEAR, true, s);
-    const bool one = p.max_batch <= FT;  // one target per thread covers every batch
-    if (precision == PREC_MIXED && KERN == KERNEL_YUKAWA && a.norb >= 4) {
-        // orbital groups share the geometry of each pair across OG orbitals
-        const bool g8 = a.norb >= 8;
-        const int gitems = p.nbatch * ((a.norb + (g8 ? 7 : 3)) / (g8 ? 8 : 4));
-        Fields a2 = an;
-        a2.out = p.near2_out;
-        if (g8) TAGI_TRY(launch_persistent(near_group<SS, 8, 0>, an, gitems, s));
-        else TAGI_TRY(launch_persistent(near_group<SS, 4, 0>, an, gitems, s));
+    if (precision == PREC_MIXED && KERN == KERNEL_YUKAWA && sh.og > 1) {
+        // orbital groups share the geometry of each pair across og orbitals
+        const bool g8 = sh.og == 8;
+        if (g8) TAGI_TRY(launch_persistent(near_group<SS, 8, 0>, wn, s));
+        else TAGI_TRY(launch_persistent(near_group<SS, 4, 0>, wn, s));
         phase_mark(PH_NEAR, false, s);
         phase_mark(PH_NEAR_CLOSE, true, s);
-        if (g8) TAGI_TRY(launch_persistent(near_group<SS, 8, 1>, a2, gitems, s));
-        else TAGI_TRY(launch_persistent(near_group<SS, 4, 1>, a2, gitems, s));
+        if (g8) TAGI_TRY(launch_persistent(near_group<SS, 8, 1>, wc, s));
+        else TAGI_TRY(launch_persistent(near_group<SS, 4, 1>, wc, s));
         phase_mark(PH_NEAR_CLOSE, false, s);
-        if (p.nslots == 0) return TAGI_OK;
         phase_mark(PH_FAR, true, s);
-        if (p.n1 <= 4) {
-            if (g8) TAGI_TRY(launch_persistent(far_group<SS, 4, 8>, af, gitems, s));
-            else TAGI_TRY(launch_persistent(far_group<SS, 4, 4>, af, gitems, s));
-        } else if (p.n1 <= 8) {
-            if (g8) TAGI_TRY(launch_persistent(far_group<SS, 8, 8>, af, gitems, s));
-            else TAGI_TRY(launch_persistent(far_group<SS, 8, 4>, af, gitems, s));
+        if (sh.maxn1 <= 4) {
+            if (g8) TAGI_TRY(launch_persistent(far_group<SS, 4, 8>, wf, s));
+            else TAGI_TRY(launch_persistent(far_group<SS, 4, 4>, wf, s));
+        } else if (sh.maxn1 <= 8) {
+            if (g8) TAGI_TRY(launch_persistent(far_group<SS, 8, 8>, wf, s));
+            else TAGI_TRY(launch_persistent(far_group<SS, 8, 4>, wf, s));
         } else {
-            if (g8) TAGI_TRY(launch_persistent(far_group<SS, MAX_DEGREE + 1, 8>, af, gitems, s));
-            else TAGI_TRY(launch_persistent(far_group<SS, MAX_DEGREE + 1, 4>, af, gitems, s));
+            if (g8) TAGI_TRY(launch_persistent(far_group<SS, MAX_DEGREE + 1, 8>, wf, s));
+            else TAGI_TRY(launch_persistent(far_group<SS, MAX_DEGREE + 1, 4>, wf, s));
         }
         phase_mark(PH_FAR, false, s);
         return TAGI_OK;
     }
     if (precision == PREC_MIXED) {
-        Fields a2 = an;
-        a2.out = p.near2_out;
-        if (one) TAGI_TRY(launch_persistent(near_mixed<KERN, SS, 1, 0>, an, items, s));
-        else TAGI_TRY(launch_persistent(near_mixed<KERN, SS, 2, 0>, an, items, s));
+        if (one) TAGI_TRY(launch_persistent(near_mixed<KERN, SS, 1, 0>, wn, s));
+        else TAGI_TRY(launch_persistent(near_mixed<KERN, SS, 2, 0>, wn, s));
         phase_mark(PH_NEAR, false, s);
         phase_mark(PH_NEAR_CLOSE, true, s);
-        if (one) TAGI_TRY(launch_persistent(near_mixed<KERN, SS, 1, 1>, a2, items, s));
-        else TAGI_TRY(launch_persistent(near_mixed<KERN, SS, 2, 1>, a2, items, s));
+        if (one) TAGI_TRY(launch_persistent(near_mixed<KERN, SS, 1, 1>, wc, s));
+        else TAGI_TRY(launch_persistent(near_mixed<KERN, SS, 2, 1>, wc, s));
         phase_mark(PH_NEAR_CLOSE, false, s);
     } else {
-        TAGI_TRY(launch_persistent(near_f64<KERN, SS>, an, items, s));
+        // one FP64 pass over all near ranges, close ones included
+        TAGI_TRY(launch_persistent(near_f64<KERN, SS>, wn, s));
         phase_mark(PH_NEAR, false, s);
     }
-    if (p.nslots == 0) return TAGI_OK;
     phase_mark(PH_FAR, true, s);
     if (precision == PREC_MIXED) {
         if (one) {
-            if (p.n1 <= 4) TAGI_TRY(launch_persistent(far_mixed<KERN, SS, 4, 1>, af, items, s));
-            else if (p.n1 <= 8) TAGI_TRY(launch_persistent(far_mixed<KERN, SS, 8, 1>, af, items, s));
-            else TAGI_TRY(launch_persistent(far_mixed<KERN, SS, MAX_DEGREE + 1, 1>, af, items, s));
+            if (sh.maxn1 <= 4) TAGI_TRY(launch_persistent(far_mixed<KERN, SS, 4, 1>, wf, s));
+            else if (sh.maxn1 <= 8) TAGI_TRY(launch_persistent(far_mixed<KERN, SS, 8, 1>, wf, s));
+            else TAGI_TRY(launch_persistent(far_mixed<KERN, SS, MAX_DEGREE + 1, 1>, wf, s));
         } else {
-            if (p.n1 <= 4) TAGI_TRY(launch_persistent(far_mixed<KERN, SS, 4, 2>, af, items, s));
-            else if (p.n1 <= 8) TAGI_TRY(launch_persistent(far_mixed<KERN, SS, 8, 2>, af, items, s));
-            else TAGI_TRY(launch_persistent(far_mixed<KERN, SS, MAX_DEGREE + 1, 2>, af, items, s));
+            if (sh.maxn1 <= 4) TAGI_TRY(launch_persistent(far_mixed<KERN, SS, 4, 2>, wf, s));
+            else if (sh.maxn1 <= 8) TAGI_TRY(launch_persistent(far_mixed<KERN, SS, 8, 2>, wf, s));
+            else TAGI_TRY(launch_persistent(far_mixed<KERN, SS, MAX_DEGREE + 1, 2>, wf, s));
         }
     } else {
-        if (p.n1 <= 4) TAGI_TRY(launch_persistent(far_f64<KERN, SS, 4>, af, items, s));
-        else if (p.n1 <= 8) TAGI_TRY(launch_persistent(far_f64<KERN, SS, 8>, af, items, s));
-        else TAGI_TRY(launch_persistent(far_f64<KERN, SS, MAX_DEGREE + 1>, af, items, s));
+        if (sh.maxn1 <= 4) TAGI_TRY(launch_persistent(far_f64<KERN, SS, 4>, wf, s));
+        else if (sh.maxn1 <= 8) TAGI_TRY(launch_persistent(far_f64<KERN, SS, 8>, wf, s));
+        else TAGI_TRY(launch_persistent(far_f64<KERN, SS, MAX_DEGREE + 1>, wf, s));
     }
     phase_mark(PH_FAR, false, s);
     return TAGI_OK;
 }
 
-}  // namespace
-
-int ensure_scratch(Plan &p, int norb) {
-    if ((size_t)norb <= p.scratch_orbitals) return TAGI_OK;
-    cudaStream_t s = p.arena.stream;
-    for (void *v : p.scratch) cudaFreeAsync(v, s);
-    p.scratch.clear();
-    p.scratch_orbitals = 0;
-    Arena a;
-    a.stream = s;
-    const size_t ns = p.src.n, nt = p.tgt.n, no = norb;
-    int rc = TAGI_OK;
-    if ((rc = a.alloc(&p.q32, no * ns)) || (rc = a.alloc(&p.ft32, no * nt)) ||
-        (rc = a.alloc(&p.q64, no * ns)) || (rc = a.alloc(&p.f64s, no * ns)) ||
-        (rc = a.alloc(&p.ft64, no * nt)) || (rc = a.alloc(&p.part, no * p.nitems * p.P)) ||
-        (rc = a.alloc(&p.qhat32, no * p.nslots * p.P)) ||
-        (rc = a.alloc(&p.qhat64, no * p.nslots * p.P)) || (rc = a.alloc(&p.near_out, no * nt)) ||
-        (rc = a.alloc(&p.near2_out, no * nt)) ||
-        (rc = a.alloc(&p.far_out, no * nt)) || (rc = a.alloc(&p.d_kc, no)) ||
-        (rc = a.alloc(&p.d_kp, no)) || (rc = a.alloc(&p.d_ss, no))) {
-        p.scratch = a.ptrs;
-        return rc;
-    }
-    p.scratch = a.ptrs;
-    p.scratch_orbitals = no;
-    return TAGI_OK;
+// Per-orbital constants from kernel parameter kp[o * nkp] (host-copied or
+// caller's device array): d_kp = k (or a), d_kc = coordinate scale sc,
+// d_ss = subtraction factor 4 pi/k^2 (Yukawa) or 2 pi/a^2 (Coulomb), 0
+// without subtraction.  A parameter the kernel cannot use sets bit 0 of err
+// and makes the orbital's subtraction factor NaN, so all its outputs are NaN.
+__global__ void orbital_constants(const double *__restrict__ kp, int nkp, int norb, int kernel, int sing,
+                                  double *__restrict__ kpo, float *__restrict__ kc, double *__restrict__ ss,
+                                  int *__restrict__ err) {
+    const int o = blockIdx.x * blockDim.x + threadIdx.x;
+    if (o >= norb) return;
+    const double k = kp[(long)o * nkp];
+    const bool used = kernel == KERNEL_YUKAWA || sing == SING_SUBTRACTION;
+    const bool bad = !isfinite(k) || (used && !(k > 0.0));
+    if (bad) atomicOr(err, 1);
+    kpo[o] = k;
+    float c = 1.0f;
+    if (kernel == KERNEL_YUKAWA) c = (float)(k * LOG2E);
+    else if (sing == SING_SUBTRACTION) c = (float)(k * sqrt(LOG2E));
+    kc[o] = c;
+    double f = 0.0;
+    if (sing == SING_SUBTRACTION) f = (kernel == KERNEL_YUKAWA ? 4.0 : 2.0) * M_PI / (k * k);
+    ss[o] = bad ? __longlong_as_double(0x7ff8000000000000LL) : f;  // NaN marks every output of the orbital
 }
 
-int convolve(Plan &p, const double *tv, const double *sv, double *out, int norb, int kernel,
-             const double *kparams, int nkp, int singularity, int precision, cudaStream_t s) {
-    TAGI_TRY(ensure_scratch(p, norb));
-    const int ns = p.src.n, nt = p.tgt.n;
-    const bool mixed = precision == PREC_MIXED;
-    const bool ss = singularity == SING_SUBTRACTION;
-
-    // Per-orbital constants: k (Yukawa) or a (Coulomb) from kernelParameters[o * nkp].
-    p.h_kc.resize(norb);
-    p.h_kp.resize(norb);
-    p.h_ss.resize(norb);
-    for (int o = 0; o < norb; o++) {
-        double k = kparams[(long)o * nkp];
-        p.h_kp[o] = k;
-        p.h_kc[o] = coordinate_scale(kernel, singularity, k);
-        p.h_ss[o] = 0.0;
-        if (ss) p.h_ss[o] = kernel == KERNEL_YUKAWA ? 4.0 * M_PI / (k * k) : 2.0 * M_PI / (k * k);
-    }
-    TAGI_CUDA(cudaMemcpyAsync(p.d_kc, p.h_kc.data(), sizeof(float) * norb, cudaMemcpyHostToDevice, s));
-    TAGI_CUDA(cudaMemcpyAsync(p.d_kp, p.h_kp.data(), sizeof(double) * norb, cudaMemcpyHostToDevice, s));
-    TAGI_CUDA(cudaMemcpyAsync(p.d_ss, p.h_ss.data(), sizeof(double) * norb, cudaMemcpyHostToDevice, s));
-
-    dim3 gs((ns + 255) / 256, norb), gt((nt + 255) / 256, norb);
-    phase_mark(PH_GLUE, true, s);
-    launch(prep_sources, gs, 256, 0, s, sv, p.src.perm, p.sw64, ns, norb, p.q32, p.q64, p.f64s);
-    launch(prep_targets, gt, 256, 0, s, tv, p.tgt.perm, nt, p.ft32, p.ft64);
-    phase_mark(PH_GLUE, false, s);
-    TAGI_LAUNCH_CHECK();
-    phase_mark(PH_UPWARD, true, s);
-    TAGI_TRY(modified_charges(p, mixed ? PREC_MIXED : PREC_FP64, norb, s));
-    if (!mixed) TAGI_TRY(ensure_weight_charges64(p, s));  // before p.what64 is read below
-    phase_mark(PH_UPWARD, false, s);
-    if (!mixed && p.nslots && !p.what64)
-        return set_error(TAGI_ERR_DEVICE, "FP64 weight charges missing");
-
+Fields make_fields(const Plan &p, int norb) {
     Fields a{};
     a.tx = p.tgt.x;
     a.ty = p.tgt.y;
@@ -1151,9 +1130,8 @@ int convolve(Plan &p, const double *tv, const double *sv, double *out, int norb,
     a.tradius = p.tgt.radius;
     a.batch_node = p.batch_node;
     a.nbatch = p.nbatch;
-    a.nt = nt;
+    a.nt = p.tgt.n;
     a.norb = norb;
-    a.queue = p.queue;
     a.rng_off = p.rng_off;
     a.rng = p.rng;
     a.rng_dmin = p.rng_dmin;
@@ -1164,7 +1142,7 @@ int convolve(Plan &p, const double *tv, const double *sv, double *out, int norb,
     a.slo = p.src_lo;
     a.thi = p.tgt_hi;
     a.tlo = p.tgt_lo;
-    a.ns = ns;
+    a.ns = p.src.n;
     a.q32 = p.q32;
     a.w32 = p.sw32;
     a.f64 = p.f64s;
@@ -1185,29 +1163,245 @@ int convolve(Plan &p, const double *tv, const double *sv, double *out, int norb,
     a.ft64 = p.ft64;
     a.kc32 = p.d_kc;
     a.kp64 = p.d_kp;
+    return a;
+}
 
-    TAGI_CUDA(cudaMemsetAsync(p.queue, 0, 3 * sizeof(int), s));
-    TAGI_CUDA(cudaMemsetAsync(p.far_out, 0, sizeof(double) * (size_t)norb * nt, s));
-    // the close-range pass writes only the targets of batches it visits; the
-    // FP64 path has a single near pass
-    TAGI_CUDA(cudaMemsetAsync(p.near2_out, 0, sizeof(double) * (size_t)norb * nt, s));
+}  // namespace
+
+bool stream_capturing(cudaStream_t s) {
+    cudaStreamCaptureStatus st = cudaStreamCaptureStatusNone;
+    if (cudaStreamIsCapturing(s, &st) != cudaSuccess) return false;
+    return st == cudaStreamCaptureStatusActive;
+}
+
+// Per-call scratch for norb orbitals.  Growing it is rare (a larger orbital
+// count than any earlier call) and synchronizes the device first: the old
+// buffers may still be in use by calls on any stream.  Plain cudaMalloc keeps
+// the new buffers valid on every stream.
+int ensure_scratch(Plan &p, int norb) {
+    if ((size_t)norb <= p.scratch_orbitals) return TAGI_OK;
+    TAGI_CUDA(cudaDeviceSynchronize());
+    for (void *v : p.scratch) cudaFree(v);
+    p.scratch.clear();
+    p.scratch_orbitals = 0;
+    const size_t ns = p.src.n, nt = p.tgt.n, no = norb;
+    auto alloc = [&](auto **ptr, size_t count) -> int {
+        void *v = nullptr;
+        const size_t bytes = (count ? count : 1) * sizeof(**ptr);
+        cudaError_t e = cudaMalloc(&v, bytes);
+        if (e != cudaSuccess)
+            return set_error(TAGI_ERR_CUDA, "device allocation of %zu bytes failed: %s", bytes, cudaGetErrorString(e));
+        p.scratch.push_back(v);
+        *ptr = static_cast<std::remove_reference_t<decltype(**ptr)> *>(v);
+        return TAGI_OK;
+    };
+    TAGI_TRY(alloc(&p.q32, no * ns));
+    TAGI_TRY(alloc(&p.ft32, no * nt));
+    TAGI_TRY(alloc(&p.q64, no * ns));
+    TAGI_TRY(alloc(&p.f64s, no * ns));
+    TAGI_TRY(alloc(&p.ft64, no * nt));
+    TAGI_TRY(alloc(&p.part, no * p.nitems * p.P));
+    TAGI_TRY(alloc(&p.qhat32, no * p.nslots * p.P));
+    TAGI_TRY(alloc(&p.qhat64, no * p.nslots * p.P));
+    TAGI_TRY(alloc(&p.near_out, no * nt));
+    TAGI_TRY(alloc(&p.near2_out, no * nt));
+    TAGI_TRY(alloc(&p.far_out, no * nt));
+    TAGI_TRY(alloc(&p.d_kc, no));
+    TAGI_TRY(alloc(&p.d_kp, no));
+    TAGI_TRY(alloc(&p.d_ss, no));
+    p.scratch_orbitals = no;
+    return TAGI_OK;
+}
+
+// Orbitals per work item: Yukawa in mixed precision shares each pair's
+// geometry across a group of 8 (or 4) orbitals once the largest system has
+// that many; everything else runs one orbital per item.  requested > 0
+// (1, 4 or 8) overrides the choice where the kernel supports it.
+int orbitals_per_item(int kernel, int precision, int max_norb, int requested) {
+    if (kernel != KERNEL_YUKAWA || precision != PREC_MIXED) return 1;
+    if (requested == 1 || requested == 4 || requested == 8) return requested;
+    return max_norb >= 8 ? 8 : (max_norb >= 4 ? 4 : 1);
+}
+
+bool schedule_matches(const Schedule &sc, const int *norb, int nsys, int og) {
+    if (sc.og != og || (int)sc.norb.size() != nsys) return false;
+    for (int i = 0; i < nsys; i++)
+        if (sc.norb[i] != norb[i]) return false;
+    return true;
+}
+
+// Work lists for one launch over nsys systems: one item per (system, batch,
+// group of og orbitals), ordered by pair count times orbitals in the item,
+// heaviest first (ties in system, batch, group order).  Passes that have
+// nothing to do for a batch (no close ranges, no far entries) get no item:
+// their outputs are cleared before the launch.
+int build_schedule(Plan *const *plans, const int *norb, int nsys, int og, Schedule &sc, cudaStream_t s) {
+    if (nsys < 1 || nsys > MAX_SYSTEMS) return set_error(TAGI_ERR_ARG, "%d systems (1..%d per launch)", nsys, MAX_SYSTEMS);
+    struct It {
+        long long cost;
+        int2 v;
+    };
+    std::vector<It> lists[3];
+    for (int i = 0; i < nsys; i++) {
+        const Plan &p = *plans[i];
+        if (norb[i] < 1 || norb[i] > 0xffff) return set_error(TAGI_ERR_ARG, "system %d: %d orbitals", i, norb[i]);
+        if ((int)p.cost_near.size() != p.nbatch) return set_error(TAGI_ERR_STATE, "plan without batch costs");
+        for (int b = 0; b < p.nbatch; b++)
+            for (int g0 = 0; g0 < norb[i]; g0 += og) {
+                const long long lanes = og;
+                const int2 v = make_int2(b, (i << 16) | g0);
+                lists[0].push_back({p.cost_near[b] * lanes, v});
+                if (p.cost_close[b] > 0) lists[1].push_back({p.cost_close[b] * lanes, v});
+                if (p.cost_far[b] > 0) lists[2].push_back({p.cost_far[b] * lanes, v});
+            }
+    }
+    std::vector<int2> all;
+    for (int k = 0; k < 3; k++) {
+        std::stable_sort(lists[k].begin(), lists[k].end(), [](const It &a, const It &b) { return a.cost > b.cost; });
+        sc.off[k] = (long)all.size();
+        sc.count[k] = (int)lists[k].size();
+        for (const It &it : lists[k]) all.push_back(it.v);
+    }
+    // the old list may be in use on any stream: wait, then replace it
+    TAGI_CUDA(cudaDeviceSynchronize());
+    sc.release();
+    if (all.empty()) all.push_back(make_int2(0, 0));
+    void *v = nullptr;
+    TAGI_CUDA(cudaMalloc(&v, sizeof(int2) * all.size()));
+    sc.items = static_cast<int2 *>(v);
+    // pageable source: the copy has read it when the call returns
+    TAGI_CUDA(cudaMemcpyAsync(sc.items, all.data(), sizeof(int2) * all.size(), cudaMemcpyHostToDevice, s));
+    sc.og = og;
+    sc.norb.assign(norb, norb + nsys);
+    return TAGI_OK;
+}
+
+// Per-orbital constants of one system into p.d_kp / d_kc / d_ss.
+static int orbital_setup(Plan &p, const SysCall &c, int kernel, int singularity, cudaStream_t s) {
+    const double *src = c.kp;
+    int stride = c.nkp;
+    if (!c.kp_device) {
+        p.h_kp.resize(c.norb);
+        for (int o = 0; o < c.norb; o++) p.h_kp[o] = c.kp[(long)o * c.nkp];
+        TAGI_CUDA(cudaMemcpyAsync(p.d_kp, p.h_kp.data(), sizeof(double) * c.norb, cudaMemcpyHostToDevice, s));
+        src = p.d_kp;
+        stride = 1;
+    }
+    launch(orbital_constants, (c.norb + 127) / 128, 128, 0, s, src, stride, c.norb, kernel, singularity, p.d_kp,
+           p.d_kc, p.d_ss, p.err_flag + 1);
+    TAGI_LAUNCH_CHECK();
+    return TAGI_OK;
+}
+
+// One convolution call over nsys systems (1..MAX_SYSTEMS) sharing kernel,
+// singularity handling and precision: per-system glue and upward pass, then
+// ONE persistent launch per field pass across all systems, then per-system
+// epilogues.  Under stream capture nothing may allocate or copy from host
+// memory: scratch, schedule and FP64 weight charges must exist already, and
+// kernel parameters must be on the device.
+int convolve_systems(SysCall *calls, int nsys, int kernel, int singularity, int precision, const Schedule &sc,
+                     int *queue, cudaStream_t s) {
+    if (nsys < 1 || nsys > MAX_SYSTEMS) return set_error(TAGI_ERR_ARG, "%d systems (1..%d per launch)", nsys, MAX_SYSTEMS);
+    const bool mixed = precision == PREC_MIXED;
+    const bool ss = singularity == SING_SUBTRACTION;
+    const bool capturing = stream_capturing(s);
+    Fields f[MAX_SYSTEMS];
+    LaunchShape sh;
+    sh.og = sc.og;
+    for (int i = 0; i < nsys; i++) {
+        SysCall &c = calls[i];
+        Plan &p = *c.p;
+        if (capturing) {
+            if ((size_t)c.norb > p.scratch_orbitals || (!mixed && p.nslots && !p.what64_ready) || !c.kp_device)
+                return set_error(TAGI_ERR_STATE,
+                                 "graph capture needs a prior uncaptured call with the same orbital counts and "
+                                 "precision, and kernel parameters on the device");
+        }
+        TAGI_TRY(ensure_scratch(p, c.norb));
+        TAGI_TRY(orbital_setup(p, c, kernel, singularity, s));
+        const int ns = p.src.n, nt = p.tgt.n;
+        dim3 gs((ns + 255) / 256, c.norb), gt((nt + 255) / 256, c.norb);
+        phase_mark(PH_GLUE, true, s);
+        launch(prep_sources, gs, 256, 0, s, c.sv, p.src.perm, p.sw64, ns, c.norb, p.q32, p.q64, p.f64s);
+        launch(prep_targets, gt, 256, 0, s, c.tv, p.tgt.perm, nt, p.ft32, p.ft64);
+        phase_mark(PH_GLUE, false, s);
+        TAGI_LAUNCH_CHECK();
+        phase_mark(PH_UPWARD, true, s);
+        TAGI_TRY(modified_charges(p, mixed ? PREC_MIXED : PREC_FP64, c.norb, s));
+        if (!mixed) TAGI_TRY(ensure_weight_charges64(p, s));  // before what64 is read below
+        phase_mark(PH_UPWARD, false, s);
+        if (!mixed && p.nslots && !p.what64) return set_error(TAGI_ERR_DEVICE, "FP64 weight charges missing");
+        f[i] = make_fields(p, c.norb);
+        if (p.max_batch > FT) sh.nt = 2;
+        if (p.n1 > sh.maxn1) sh.maxn1 = p.n1;
+        // the far and close-range passes write only the batches they visit
+        TAGI_CUDA(cudaMemsetAsync(p.far_out, 0, sizeof(double) * (size_t)c.norb * nt, s));
+        TAGI_CUDA(cudaMemsetAsync(p.near2_out, 0, sizeof(double) * (size_t)c.norb * nt, s));
+    }
+    TAGI_CUDA(cudaMemsetAsync(queue, 0, 3 * sizeof(int), s));
     if (kernel == KERNEL_YUKAWA) {
-        if (ss) TAGI_TRY((launch_fields<KERNEL_YUKAWA, true>(p, a, precision, s)));
-        else TAGI_TRY((launch_fields<KERNEL_YUKAWA, false>(p, a, precision, s)));
+        if (ss) TAGI_TRY((launch_fields<KERNEL_YUKAWA, true>(calls, f, nsys, sc, sh, precision, queue, s)));
+        else TAGI_TRY((launch_fields<KERNEL_YUKAWA, false>(calls, f, nsys, sc, sh, precision, queue, s)));
     } else {
-        if (ss) TAGI_TRY((launch_fields<KERNEL_COULOMB, true>(p, a, precision, s)));
-        else TAGI_TRY((launch_fields<KERNEL_COULOMB, false>(p, a, precision, s)));
+        if (ss) TAGI_TRY((launch_fields<KERNEL_COULOMB, true>(calls, f, nsys, sc, sh, precision, queue, s)));
+        else TAGI_TRY((launch_fields<KERNEL_COULOMB, false>(calls, f, nsys, sc, sh, precision, queue, s)));
     }
     phase_mark(PH_GLUE, true, s);
-    if (mixed)
-        launch(epilogue<float>, gt, 256, 0, s, p.near_out, p.near2_out, p.far_out, p.ft32, p.tgt.perm, nt, p.d_ss,
-               out);
-    else
-        launch(epilogue<double>, gt, 256, 0, s, p.near_out, p.near2_out, p.far_out, p.ft64, p.tgt.perm, nt, p.d_ss,
-               out);
+    for (int i = 0; i < nsys; i++) {
+        const SysCall &c = calls[i];
+        const Plan &p = *c.p;
+        const int nt = p.tgt.n;
+        dim3 gt((nt + 255) / 256, c.norb);
+        if (mixed)
+            launch(epilogue<float>, gt, 256, 0, s, p.near_out, p.near2_out, p.far_out, p.ft32, p.tgt.perm, nt,
+                   p.d_ss, c.out);
+        else
+            launch(epilogue<double>, gt, 256, 0, s, p.near_out, p.near2_out, p.far_out, p.ft64, p.tgt.perm, nt,
+                   p.d_ss, c.out);
+    }
     phase_mark(PH_GLUE, false, s);
     TAGI_LAUNCH_CHECK();
     return TAGI_OK;
+}
+
+// Single-plan call (norb orbitals over one mesh) with the plan's cached
+// work list.
+int convolve(Plan &p, const double *tv, const double *sv, double *out, int norb, int kernel,
+             const double *kparams, int nkp, int singularity, int precision, cudaStream_t s, bool kp_device,
+             int og_request) {
+    const int og = orbitals_per_item(kernel, precision, norb, og_request);
+    const Schedule *sc = nullptr;
+    for (const Schedule &c : p.scheds)
+        if (schedule_matches(c, &norb, 1, og)) sc = &c;
+    if (!sc) {
+        if (stream_capturing(s))
+            return set_error(TAGI_ERR_STATE, "graph capture needs a prior uncaptured call with the same orbital count");
+        constexpr size_t KEEP = 4;  // work lists kept per plan (e.g. Hartree + orbital batch)
+        if (p.scheds.size() >= KEEP) {
+            TAGI_CUDA(cudaDeviceSynchronize());
+            p.scheds.front().release();
+            p.scheds.erase(p.scheds.begin());
+        }
+        p.scheds.emplace_back();
+        Plan *pp = &p;
+        const int rc = build_schedule(&pp, &norb, 1, og, p.scheds.back(), s);
+        if (rc) {
+            p.scheds.back().release();
+            p.scheds.pop_back();
+            return rc;
+        }
+        sc = &p.scheds.back();
+    }
+    SysCall c;
+    c.p = &p;
+    c.tv = tv;
+    c.sv = sv;
+    c.out = out;
+    c.norb = norb;
+    c.kp = kparams;
+    c.nkp = nkp;
+    c.kp_device = kp_device;
+    return convolve_systems(&c, 1, kernel, singularity, precision, *sc, p.queue, s);
 }
 
 int pair_peak(int kernel, int singularity, int variant, double kp, double *pairs_per_s, cudaStream_t s) {

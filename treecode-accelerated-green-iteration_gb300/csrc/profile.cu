@@ -27,6 +27,7 @@ void count_launch() { g_launches.fetch_add(1, std::memory_order_relaxed); }
 
 void phase_mark(int phase, bool begin, cudaStream_t s) {
     if (!g_profile.load(std::memory_order_relaxed) || phase < 0 || phase >= PH_COUNT) return;
+    if (stream_capturing(s)) return;  // events inside a graph would be read before they run
     std::lock_guard<std::mutex> lk(g_pmu);
     cudaEvent_t e;
     if (cudaEventCreate(&e) != cudaSuccess) return;

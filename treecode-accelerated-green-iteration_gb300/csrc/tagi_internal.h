@@ -34,6 +34,10 @@ constexpr int TRAVERSAL_STACK = 256;  // DFS stack entries per target batch
 
 int set_error(int code, const char *fmt, ...);
 int last_error();
+// Argument checks shared by the C entry points (capi.cu).
+int validate(int nt, int ns, int kernel, int nkp, const double *kp, int sing, int approx, int ctype, double theta,
+             int degree, int sl, int tl, double size_check, int precision);
+int validate_kparam(int kernel, int sing, double k);
 
 #define TAGI_CUDA(call)                                                                   \
     do {                                                                                  \
@@ -112,6 +116,24 @@ struct Tree {
     double *center = nullptr, *half = nullptr, *radius = nullptr;
 };
 
+// Work list of one field launch: items {batch, sys << 16 | first orbital},
+// heaviest first, in three segments: near pass 0 (every batch), near close
+// pass (batches with close ranges), far field (batches with far entries).
+// og orbitals per item (orbital-group kernels) or 1.
+struct Schedule {
+    int og = 0;                 // 0 = not built
+    std::vector<int> norb;      // orbitals per system the schedule was built for
+    int2 *items = nullptr;      // device, owned
+    int count[3] = {0, 0, 0};
+    long off[3] = {0, 0, 0};
+    void release() {  // caller makes sure no launch still reads the list
+        if (items) cudaFree(items);
+        items = nullptr;
+        og = 0;
+        norb.clear();
+    }
+};
+
 struct Plan {
     int device = 0;
     Arena arena;
@@ -142,9 +164,8 @@ struct Plan {
     float *what32 = nullptr;               // weight modified charges [slot][P]
     double *what64 = nullptr;              // FP64 set, built on first FP64 use
     bool what64_ready = false;
-    int *order_near = nullptr, *order_far = nullptr;   // batches, heaviest first
     int *queue = nullptr;                  // work-queue counters (3 ints)
-    int *err_flag = nullptr;
+    int *err_flag = nullptr;               // [0] tree/list build, [1] unusable kernel parameter
     double cheb[MAX_DEGREE + 1];           // cos(m pi / degree)
     // per-convolution scratch (grown on demand)
     size_t scratch_orbitals = 0;
@@ -166,7 +187,28 @@ struct Plan {
     // statistics (host)
     double near_pairs = 0, far_pairs = 0;  // pair interactions per orbital
     double near_close_pairs = 0;           // part of near_pairs in close ranges
+    // per-batch pair counts (host) for work ordering: ordinary near ranges,
+    // close ranges, far field
+    std::vector<long long> cost_near, cost_close, cost_far;
+    std::vector<Schedule> scheds;          // single-plan work lists by (orbitals, group), cached
 };
+
+// One system of a (possibly multi-system) convolution call.
+struct SysCall {
+    Plan *p = nullptr;
+    const double *tv = nullptr, *sv = nullptr;  // device [norb][nt], [norb][ns], caller order
+    double *out = nullptr;                      // device [norb][nt], caller order
+    int norb = 1;
+    const double *kp = nullptr;  // kernel parameters: k (or a) of orbital o at kp[o * nkp]
+    int nkp = 1;
+    bool kp_device = false;      // kp is a device pointer (graph-capturable calls)
+};
+
+struct Plan;
+int plan_create(Plan **out, int nt, const double *tx, const double *ty, const double *tz, int ns,
+                const double *sx, const double *sy, const double *sz, const double *sw, double theta, int degree,
+                int sl, int tl, double size_check, cudaStream_t s);
+void plan_destroy(Plan *p);
 
 // scan_sort.cu
 int exclusive_scan(const int *in, int *out, int n, int *d_total, Arena &ar, cudaStream_t s);
@@ -183,9 +225,17 @@ int ensure_weight_charges64(Plan &p, cudaStream_t s);
 int modified_charges(Plan &p, int precision, int norb, cudaStream_t s);
 
 // fields.cu
+constexpr int MAX_SYSTEMS = 8;  // systems per field launch
 int ensure_scratch(Plan &p, int norb);
+int orbitals_per_item(int kernel, int precision, int max_norb, int requested);
+int build_schedule(Plan *const *plans, const int *norb, int nsys, int og, Schedule &sc, cudaStream_t s);
+bool schedule_matches(const Schedule &sc, const int *norb, int nsys, int og);
+int convolve_systems(SysCall *calls, int nsys, int kernel, int singularity, int precision,
+                     const Schedule &sc, int *queue, cudaStream_t s);
 int convolve(Plan &p, const double *tv, const double *sv, double *out, int norb, int kernel,
-             const double *kparams, int nkp, int singularity, int precision, cudaStream_t s);
+             const double *kparams, int nkp, int singularity, int precision, cudaStream_t s,
+             bool kp_device = false, int og_request = 0);
+bool stream_capturing(cudaStream_t s);
 int direct_sum(int nt, const double *tx, const double *ty, const double *tz, const double *tv,
                int nsub, const int *sub, int ns, const double *sx, const double *sy,
                const double *sz, const double *sv, const double *sw, double *out, int kernel,

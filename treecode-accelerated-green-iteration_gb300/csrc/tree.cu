@@ -707,7 +707,7 @@ int build_lists(Plan &p, cudaStream_t s) {
                                                               p.src.end, P2M_CHUNK, p.slot_item_off,
                                                               p.item_slot, p.item_begin, p.item_end);
 
-        // Work order for the field kernels: heaviest batch first.
+        // Per-batch pair counts: the field kernels' work lists go heaviest first.
         long long *cn = nullptr, *cf = nullptr, *cc2 = nullptr;
         int *bsz = nullptr;
         if ((rc = tmp.alloc(&cn, nb)) || (rc = tmp.alloc(&cf, nb)) || (rc = tmp.alloc(&bsz, nb)) ||
@@ -729,23 +729,17 @@ int build_lists(Plan &p, cudaStream_t s) {
         p.near_close_pairs = 0;
         p.far_pairs = 0;
         p.max_batch = 0;
+        p.cost_near.resize(nb);
+        p.cost_close.resize(nb);
+        p.cost_far.resize(nb);
         for (int b = 0; b < nb; b++) {
             p.near_pairs += (double)hcn[b];
             p.near_close_pairs += (double)hcc[b];
             p.far_pairs += (double)hcf[b] * p.P;
             p.max_batch = std::max(p.max_batch, hsz[b]);
-        }
-        std::vector<int> on(nb), of(nb);
-        std::iota(on.begin(), on.end(), 0);
-        std::iota(of.begin(), of.end(), 0);
-        std::stable_sort(on.begin(), on.end(), [&](int a, int b) { return hcn[a] > hcn[b]; });
-        std::stable_sort(of.begin(), of.end(), [&](int a, int b) { return hcf[a] > hcf[b]; });
-        if ((rc = ar.alloc(&p.order_near, nb)) || (rc = ar.alloc(&p.order_far, nb))) break;
-        if (cudaMemcpyAsync(p.order_near, on.data(), sizeof(int) * nb, cudaMemcpyHostToDevice, s) ||
-            cudaMemcpyAsync(p.order_far, of.data(), sizeof(int) * nb, cudaMemcpyHostToDevice, s) ||
-            cudaStreamSynchronize(s)) {
-            rc = set_error(TAGI_ERR_CUDA, "batch order upload failed");
-            break;
+            p.cost_near[b] = hcn[b] - hcc[b];
+            p.cost_close[b] = hcc[b];
+            p.cost_far[b] = hcf[b] * (long long)p.P;
         }
         if (cudaGetLastError() != cudaSuccess) { rc = set_error(TAGI_ERR_CUDA, "list kernels failed"); break; }
     } while (0);

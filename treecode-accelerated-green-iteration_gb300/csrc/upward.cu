@@ -185,7 +185,13 @@ int build_weight_charges(Plan &p, cudaStream_t s) {
 
 int ensure_weight_charges64(Plan &p, cudaStream_t s) {
     if (p.what64_ready) return TAGI_OK;
-    if (!p.what64) TAGI_TRY(p.arena.alloc(&p.what64, (size_t)p.nslots * p.P));
+    if (!p.what64) {
+        // plain cudaMalloc: the first FP64 call may run on another stream than the plan's
+        void *v = nullptr;
+        TAGI_CUDA(cudaMalloc(&v, sizeof(double) * ((size_t)p.nslots * p.P + 1)));
+        p.arena.ptrs.push_back(v);
+        p.what64 = static_cast<double *>(v);
+    }
     if (p.nslots) {
         Arena tmp;
         tmp.stream = s;
