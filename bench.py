@@ -14,7 +14,16 @@ convolutions/s over all ranks.  ``e2e`` = the same through the C ABI
 device allocation and the device->host result copy are inside the timing.
 
   python bench.py [--gpus N] [--steps K] [--warmup W] [--impl gb300|reference]
-                  [--workload hartree|orbitals]
+                  [--workload hartree|orbitals|uneven]
+
+``--workload uneven``: six independent synthetic systems (50k .. 2.5M points,
+4/8/8/16/32/64 orbitals, Yukawa with subtraction, k_i ~ U[0.4, 3]) convolved
+together, all orbitals of all systems in one persistent launch per field pass,
+the launch sequence captured once as a CUDA graph and replayed; leaf sizes and
+kernel shape chosen by the autotuner (untimed).  One step = one replay: one
+Green-iteration sweep's convolutions (plans reused, as Green iteration reuses
+them).  Compared with the plain path: one FP64 tagi_treecode_dev call per
+orbital (tree + convolution each, reference parameters: leaves 500).
 
 ``--impl reference`` times the CPU FP64 restatement of the same treecode (the
 reference's BaryTree is not available) on the host cores, on a bounded sample
@@ -50,7 +59,9 @@ def parse():
     ap.add_argument("--steps", type=int, default=5)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
-    ap.add_argument("--workload", default="hartree", choices=["hartree", "orbitals"])
+    ap.add_argument("--workload", default="hartree", choices=["hartree", "orbitals", "uneven"])
+    ap.add_argument("--fp64-sample-systems", type=int, default=2,
+                    help="uneven workload: systems whose plain FP64 one-call-per-orbital time is measured")
     ap.add_argument("--cpu-seconds", type=float, default=15.0,
                     help="target CPU seconds of field work per CPU-baseline sample")
     ap.add_argument("--no-cpu-baseline", action="store_true")
@@ -147,14 +158,14 @@ class ClockSampler:
 # ---------------------------------------------------------------------------
 # CPU baseline: the FP64 treecode restatement on the host cores
 # ---------------------------------------------------------------------------
-def cpu_treecode_sample(wl, target_seconds, threads):
+def cpu_treecode_sample(wl, target_seconds, threads, leaf=None):
     """Build the CPU plan (timed), convolve a sample of whole target batches
     sized to ~target_seconds of field work, extrapolate to one convolution by
     the pair counts of the full lists.  Returns (seconds per convolution, info)."""
     from oracle import oracle as O
     O.build()
     mesh = wl["mesh"]
-    sl, tl = LEAF["hartree"]
+    sl, tl = leaf or LEAF["hartree"]
     t0 = time.perf_counter()
     plan = O.Plan(mesh.x, mesh.y, mesh.z, mesh.x, mesh.y, mesh.z, mesh.w, THETA, DEGREE, sl, tl, 1.0)
     t_plan = time.perf_counter() - t0
@@ -187,7 +198,7 @@ def cpu_treecode_sample(wl, target_seconds, threads):
     seconds = t_plan + t_up + t_f / frac
     return seconds, dict(batches=int(nsel), of_batches=int(nb), pair_fraction=float(frac),
                          plan_s=t_plan, upward_s=t_up, sample_field_s=t_f,
-                         pairs_per_s=(pn + pf) / t_f)
+                         pairs_per_s=(pn + pf) / t_f, total_pairs=float(total_pairs))
 
 
 def reference_arm(args):
@@ -409,10 +420,229 @@ def gb300_arm(args):
     return 0
 
 
+# ---------------------------------------------------------------------------
+# Uneven multi-system batch: one persistent launch per pass, CUDA graph
+# ---------------------------------------------------------------------------
+UNEVEN_LEAVES = ((1000, 1000), (2000, 1000), (2000, 2000), (4000, 2000))
+PLAIN_LEAF = 500  # the reference's callers pass 500-point leaves (BASELINE config 1 parameters)
+
+
+def uneven_arm(args):
+    import torch
+    import torch.distributed as dist
+
+    ws, rank, local = dist_env()
+    torch.cuda.set_device(local)
+    if ws > 1:
+        dist.init_process_group("nccl", device_id=torch.device("cuda", local))
+    pkg = importlib.import_module(PKG)
+    dev = importlib.import_module(PKG + ".device")
+    tune = importlib.import_module(PKG + ".autotune")
+    nat = pkg._native
+    L = nat.lib()
+    BT = pkg.BaryTreeInterface
+    K, SS = BT.Kernel.YUKAWA, BT.Singularity.SUBTRACTION
+    cuda = torch.device("cuda", local)
+    t = lambda a: torch.as_tensor(np.ascontiguousarray(a), dtype=torch.float64, device=cuda)
+    systems = pkg.synthetic.uneven_systems(seed=4)
+    meshes = [(t(m.x), t(m.y), t(m.z), t(m.w)) for m, _, _ in systems]
+    vals = [t(F) for _, F, _ in systems]
+    ks = [np.asarray(k, dtype=np.float64) for _, _, k in systems]
+    norbs = [int(F.shape[0]) for _, F, _ in systems]
+    npts = [int(m.n) for m, _, _ in systems]
+
+    # autotuner (untimed): leaves per system, joint kernel shape
+    t0 = time.perf_counter()
+    tuned = tune.tune_systems(meshes, vals, ks, K, SS, precision="mixed", theta=THETA, degree=DEGREE,
+                              leaves=UNEVEN_LEAVES, reuse=50, tol=1e-6, sample_orbitals=4)
+    tune_s = time.perf_counter() - t0
+    plans = [dev.TreecodePlan.for_mesh(*mesh, theta=THETA, degree=DEGREE, source_leaf=sl, target_leaf=tl)
+             for mesh, (sl, tl) in zip(meshes, tuned["leaves"])]
+    S = dev.Systems(plans, norbs, K, precision="mixed", orbitals_per_item=tuned["orbitals_per_item"],
+                    targets_per_thread=tuned["targets_per_thread"])
+    kdev = [t(k) for k in ks]
+    outs = [torch.empty_like(v) for v in vals]
+    stream = torch.cuda.Stream()
+    torch.cuda.synchronize()
+    with torch.cuda.stream(stream):
+        S.convolve(vals, vals, kdev, SS, outs=outs, stream=stream)  # uncaptured first call
+        with dev.Graph.capture(stream) as graph:
+            S.convolve(vals, vals, kdev, SS, outs=outs, stream=stream)
+        for _ in range(args.warmup):
+            graph.replay(stream)
+        stream.synchronize()
+        flush = torch.empty(64 * 1024 * 1024, dtype=torch.float32, device=cuda)  # 256 MB > L2
+        evs = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True))
+               for _ in range(args.steps)]
+        with ClockSampler(local) as clocks:
+            if ws > 1:
+                dist.barrier()
+            torch.cuda.synchronize()
+            n0 = L.tagi_launch_count()
+            for k in range(args.steps):
+                flush.zero_()
+                evs[k][0].record(stream)
+                graph.replay(stream)
+                evs[k][1].record(stream)
+            torch.cuda.synchronize()
+            if ws > 1:
+                dist.barrier()
+    n_nodes = graph.nodes()
+    # launches inside the timed region: every replay runs the captured kernels
+    launches_per_replay = None
+    step_ms = [a.elapsed_time(b) for a, b in evs]
+    total_ms = float(sum(step_ms))
+    if ws > 1:
+        tt = torch.tensor([total_ms], device=cuda)
+        dist.all_reduce(tt, op=dist.ReduceOp.MAX)
+        total_ms = float(tt.item())
+    orb_total = sum(norbs)
+    value = orb_total * args.steps * ws / (total_ms * 1e-3)
+    if rank != 0:
+        if ws > 1:
+            dist.destroy_process_group()
+        return 0
+
+    # per-pass device times from one profiled uncaptured call
+    L.tagi_profile(1)
+    prof_ms = np.zeros(7)
+    prof_n = np.zeros(7, dtype=np.int64)
+    prof_np = prof_n.ctypes.data_as(ctypes.POINTER(ctypes.c_longlong))
+    L.tagi_profile_read(nat.dptr(prof_ms), prof_np, 7)
+    c0 = L.tagi_launch_count()
+    S.convolve(vals, vals, kdev, SS, outs=outs)
+    torch.cuda.synchronize()
+    launches_per_replay = int(L.tagi_launch_count() - c0)
+    L.tagi_profile_read(nat.dptr(prof_ms), prof_np, 7)
+    L.tagi_profile(0)
+
+    # accuracy: first and last orbital of every system at 1024 seeded targets vs FP64 direct sum
+    rng = np.random.default_rng(99)
+    errs = []
+    for (x, y, z, w), v, k, o, n in zip(meshes, vals, ks, outs, npts):
+        sub = torch.as_tensor(np.sort(rng.choice(n, min(1024, n), replace=False)).astype(np.int32), device=cuda)
+        for j in (0, v.shape[0] - 1):
+            vj = v[j].contiguous()
+            ref = dev.direct(x, y, z, vj, x, y, z, vj, w, K, [k[j]], SS, subset=sub)
+            errs.append(float(torch.linalg.norm(o[j][sub.long()] - ref) / torch.linalg.norm(ref)))
+
+    # pair counts and roofline of the dominant pass (near, orbital groups)
+    infos = [p.info() for p in plans]
+    pairs_near = sum((i["near_pairs"] - i["near_close_pairs"]) * no for i, no in zip(infos, norbs))
+    pairs_far = sum(i["far_pairs"] * no for i, no in zip(infos, norbs))
+    pairs_all = sum((i["near_pairs"] + i["far_pairs"]) * no for i, no in zip(infos, norbs))
+    near_ms, far_ms = prof_ms[3], prof_ms[4]
+    og = S.info()["orbitals_per_item"]
+    peak = ctypes.c_double()
+    nat.check(L.tagi_pair_peak(int(K), int(SS), 2 if og > 1 else 0, 1.0, ctypes.byref(peak),
+                               ctypes.c_void_p(torch.cuda.current_stream().cuda_stream)))
+    achieved = pairs_near / (near_ms * 1e-3)
+    roofline = {"bound": "mufu", "achieved": achieved / 1e9, "peak": peak.value / 1e9, "unit": "Gpair/s",
+                "frac": achieved / peak.value, "traffic": None,
+                "kernel": f"near_group<OG={og}> over all systems" if og > 1 else "near_mixed over all systems",
+                "peak_source": "tagi_pair_peak variant 2 (orbital-group near loop, 8 orbitals per pair "
+                               "geometry), measured live on this GPU" if og > 1 else "tagi_pair_peak variant 0",
+                "kernel_ms_per_launch": near_ms, "pairs_per_launch": pairs_near,
+                "far_ms_per_launch": far_ms, "far_pairs_per_launch": pairs_far}
+
+    # plain path: one FP64 tagi_treecode_dev call per orbital (tree + convolution), leaves 500
+    plain = []
+    for i in range(min(args.fp64_sample_systems, len(systems))):
+        x, y, z, w = meshes[i]
+        v0 = vals[i][0].contiguous()
+        torch.cuda.synchronize()
+        a = time.perf_counter()
+        dev.treecode(x, y, z, v0, x, y, z, v0, w, K, [ks[i][0]], SS, THETA, DEGREE, PLAIN_LEAF, PLAIN_LEAF,
+                     precision="fp64")
+        torch.cuda.synchronize()
+        plain.append(time.perf_counter() - a)
+    # pair counts of the plain trees (plan only) to extend the measured FP64 rate to every system
+    plain_pairs = []
+    for mesh in meshes:
+        p = dev.TreecodePlan.for_mesh(*mesh, theta=THETA, degree=DEGREE, source_leaf=PLAIN_LEAF,
+                                      target_leaf=PLAIN_LEAF)
+        inf = p.info()
+        plain_pairs.append(inf["near_pairs"] + inf["far_pairs"])
+        p.close()
+    rate64 = sum(plain_pairs[:len(plain)]) / sum(plain)
+    plain_s = sum(no * (plain[i] if i < len(plain) else plain_pairs[i] / rate64)
+                  for i, no in enumerate(norbs))
+    plain_value = orb_total / plain_s
+
+    # end to end: host arrays -> tagi_treecode_batched (plans, tuned leaves per call) -> host
+    off = np.concatenate([[0], np.cumsum(npts)]).astype(np.int32)
+    hx, hy, hz, hw = (torch.as_tensor(np.concatenate([getattr(m, a) for m, _, _ in systems])).pin_memory()
+                      for a in "xyzw")
+    hv = torch.as_tensor(np.concatenate([F.reshape(-1) for _, F, _ in systems])).pin_memory()
+    kall = np.concatenate(ks)
+    hout = torch.empty_like(hv).pin_memory()
+    sl_e, tl_e = tuned["leaves"][-1]  # the largest system's leaves (one leaf setting per one-shot call)
+    torch.cuda.synchronize()
+    a = time.perf_counter()
+    dx, dy, dz, dw, dv = (h.to(cuda, non_blocking=True) for h in (hx, hy, hz, hw, hv))
+    dout = dev.treecode_batched(off, norbs, dx, dy, dz, dw, dv, K, kall, SS, theta=THETA, degree=DEGREE,
+                                source_leaf=sl_e, target_leaf=tl_e, precision="mixed")
+    hout.copy_(dout, non_blocking=True)
+    torch.cuda.synchronize()
+    e2e_s = time.perf_counter() - a
+    e2e = {"value": orb_total / e2e_s, "unit": "orbital convolutions/s",
+           "h2d_bytes_per_step": int(8 * (4 * off[-1] + hv.numel())), "d2h_bytes_per_step": int(8 * hout.numel()),
+           "path": "tagi_treecode_batched (one-shot: plans built inside the call), pinned host buffers"}
+
+    cpu = None
+    if not args.no_cpu_baseline and ws == 1:
+        threads = os.cpu_count() or 1
+        i = 2  # 300k-point system: CPU FP64 pair rate on a sample of its batches
+        m, F, k = systems[i]
+        wl = dict(mesh=m, values=F, kparams=k[:, None], kernel=K, singularity=SS)
+        secs, cinfo = cpu_treecode_sample(wl, args.cpu_seconds, threads, leaf=tuned["leaves"][i])
+        rate = cinfo["pairs_per_s"]
+        cpu_s = sum(no * (i_["near_pairs"] + i_["far_pairs"]) / rate for i_, no in zip(infos, norbs))
+        cpu = {"value": orb_total / cpu_s, "unit": "orbital convolutions/s", "cores": threads, "kind": "port",
+               "sample": (f"FP64 treecode restatement on {cinfo['batches']} of {cinfo['of_batches']} batches "
+                          f"of the {m.n}-point system (one orbital); its pair rate "
+                          f"{rate:.3g}/s applied to all {orb_total} orbital convolutions' pair counts")}
+
+    clk = clocks.summary()
+    line = {
+        "metric": METRIC, "value": value, "unit": "orbital convolutions/s", "n_gpus": ws, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": total_ms / args.steps, "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f32+f64", "data": "synthetic (seeded meshes and orbitals)",
+        "config": {"workload": "uneven_6_systems_yukawa_ss", "points": npts, "orbitals": norbs,
+                   "theta": THETA, "degree": DEGREE, "precision": "mixed",
+                   "step": "one CUDA-graph replay: all orbitals of all systems, one persistent launch per field "
+                           "pass; plans reused",
+                   "graph_nodes": n_nodes, "l2": "256 MB buffer written between timed steps (untimed)",
+                   "autotune": {"leaves": tuned["leaves"], "orbitals_per_item": tuned["orbitals_per_item"],
+                                "targets_per_thread": tuned["targets_per_thread"], "seconds": tune_s,
+                                "joint": tuned["joint"]},
+                   "rel_l2_vs_fp64_direct_max": max(errs), "rel_l2_checks": len(errs),
+                   "pairs_per_step": pairs_all},
+        "phase_ms_uncaptured_call": {k_: float(v_) for k_, v_ in zip(
+            ("tree", "lists", "upward", "near", "far", "glue", "near_close"), prof_ms)},
+        "plain_fp64_one_call_per_orbital": {
+            "value": plain_value, "unit": "orbital convolutions/s",
+            "measured_systems": len(plain), "seconds_per_orbital_measured": plain,
+            "fp64_pairs_per_s": rate64, "speedup_of_batched": value / plain_value,
+            "note": "systems beyond the measured ones extrapolated by their plain-tree pair counts"},
+        "roofline": roofline, "cpu_baseline": cpu, "e2e": e2e, "clocks": clk,
+        "gpu_launches": launches_per_replay * args.steps,
+    }
+    print(json.dumps(line), flush=True)
+    S.close()
+    for p in plans:
+        p.close()
+    if ws > 1:
+        dist.destroy_process_group()
+    return 0
+
+
 def main():
     args = parse()
     if args.impl == "reference":
         return reference_arm(args)
+    if args.workload == "uneven":
+        return uneven_arm(args)
     return gb300_arm(args)
 
 

@@ -141,12 +141,14 @@ int tagi_plan_convolve(tagi_plan *plan, int numOrbitals, const double *targetVal
  * gives NaN output and sets a flag that tagi_plan_check_parameters returns.
  * orbitalsPerItem: 0 = automatic, 1, 4 or 8 (Yukawa mixed precision shares
  * each pair's geometry across a group of orbitals; other cases use 1).
+ * targetsPerThread: 0 = automatic (2 when a batch exceeds 256 targets), 1 or
+ * 2 (mixed single-orbital field kernels; a tuning knob, results unchanged).
  * Extends callTreedriver (BaryTreeInterface.py:88-158), which has neither. */
 int tagi_plan_convolve_ex(tagi_plan *plan, int numOrbitals, const double *targetValues,
                           const double *sourceValues, double *output, int kernel,
                           int numberOfKernelParameters, const double *kernelParameters,
                           int kernelParametersOnDevice, int singularity, int precision,
-                          int orbitalsPerItem, void *stream);
+                          int orbitalsPerItem, int targetsPerThread, void *stream);
 /* Waits for the stream, returns (and clears) the plan's flag of unusable
  * device kernel parameters: *flags != 0 if any call since the last check
  * had one. */
@@ -162,7 +164,7 @@ int tagi_plan_check_parameters(tagi_plan *plan, int *flags, void *stream);
 typedef struct tagi_systems tagi_systems;
 int tagi_systems_create(tagi_systems **systems, int numSystems, tagi_plan *const *plans,
                         const int *numOrbitals, int kernel, int precision, int orbitalsPerItem,
-                        void *stream);
+                        int targetsPerThread, void *stream);
 /* Arrays of numSystems device pointers, each laid out as tagi_plan_convolve's
  * arguments for that system; kernelParameters[i] host or device (flag). */
 int tagi_systems_convolve(tagi_systems *systems, const double *const *targetValues,
@@ -268,8 +270,9 @@ int tagi_beta_parameters(double beta, double *theta, int *degree, int *sourceLea
 long long tagi_launch_count(void);
 /* Pair-throughput ceiling of the mixed-precision field kernels on this GPU:
  * their inner-loop arithmetic (variant 0: near-field loop, 1: far-field
- * proxy-grid loop) with operands in shared memory and registers and no
- * global-memory traffic, timed with CUDA events.  Pair interactions / s. */
+ * proxy-grid loop, 2: Yukawa orbital-group near loop, 8 orbitals per pair,
+ * counted per pair and orbital) with operands in shared memory and registers
+ * and no global-memory traffic, timed with CUDA events.  Pair interactions / s. */
 int tagi_pair_peak(int kernel, int singularity, int variant, double kernelParameter,
                    double *pairsPerSecond, void *stream);
 int tagi_profile(int enable);

@@ -151,3 +151,40 @@ def test_capture_without_prior_call_is_refused(BT, dev, native, systems):
         stream.synchronize()
     assert torch.isfinite(out).all()
     fresh.close()
+
+
+def test_targets_per_thread_does_not_change_results(BT, systems):
+    mesh, F, k, plan = systems[2]
+    (Ft,) = to_cuda(F[:2])
+    a = plan.convolve(Ft, Ft, BT.Kernel.YUKAWA, k[:2], BT.Singularity.SUBTRACTION, orbitals_per_item=1,
+                      targets_per_thread=1)
+    b = plan.convolve(Ft, Ft, BT.Kernel.YUKAWA, k[:2], BT.Singularity.SUBTRACTION, orbitals_per_item=1,
+                      targets_per_thread=2)
+    assert torch.equal(a, b)
+
+
+def test_autotune_picks_a_candidate_within_tolerance(BT, pkg, systems, tmp_path):
+    import importlib
+    tune = importlib.import_module(pkg.__name__ + ".autotune")
+    mesh, F, k, _ = systems[2]
+    x, y, z, w, Ft = to_cuda(mesh.x, mesh.y, mesh.z, mesh.w, F)
+    cache = str(tmp_path / "tune.json")
+    r = tune.tune(x, y, z, w, Ft, BT.Kernel.YUKAWA, k, BT.Singularity.SUBTRACTION,
+                  leaves=((300, 300), (600, 300)), sample_orbitals=4, repeats=1, n_check=512, tol=1e-5,
+                  cache_path=cache)
+    assert r["met_tol"] and r["rel_err"] <= 1e-5 and not r["cached"]
+    assert (r["source_leaf"], r["target_leaf"]) in ((300, 300), (600, 300))
+    assert r["orbitals_per_item"] in (0, 1, 4) and r["targets_per_thread"] in (0, 1, 2)
+    assert len(r["table"]) == 2 + 2 * 2  # two trees, then groups {1, 4} x targets per thread {1, 2}
+    again = tune.tune(x, y, z, w, Ft, BT.Kernel.YUKAWA, k, BT.Singularity.SUBTRACTION,
+                      leaves=((300, 300), (600, 300)), sample_orbitals=4, tol=1e-5, cache_path=cache)
+    assert again["cached"] and again["source_leaf"] == r["source_leaf"]
+
+
+def test_group_pair_ceiling_is_measured(native):
+    import ctypes
+    L = native.lib()
+    v = ctypes.c_double()
+    native.check(L.tagi_pair_peak(2, 2, 2, 1.0, ctypes.byref(v), None))
+    assert v.value > 1e11
+    assert L.tagi_pair_peak(1, 2, 2, 1.0, ctypes.byref(v), None) == native.TAGI_ERR_UNSUPPORTED

@@ -5,8 +5,9 @@ Reference-facing modules (same names and call signatures as
   BaryTreeInterface          callTreedriver + enums
   orthogonalization_wrapper  callOrthogonalization
   interpolation_wrapper      callInterpolator
-Device API over torch CUDA tensors: device (TreecodePlan, treecode, direct,
-mgs, interp).  Synthetic seeded workloads: synthetic.  Build: build.
+Device API over torch CUDA tensors: device (TreecodePlan, Systems, Graph,
+treecode, treecode_batched, direct, mgs, interp).  Launch-shape tuning:
+autotune.  Synthetic seeded workloads: synthetic.  Build: build.
 
 TAGI imports these modules by name after putting the utilities directory on
 sys.path; putting this directory on sys.path does the same here.
@@ -15,4 +16,4 @@ from . import BaryTreeInterface, interpolation_wrapper, orthogonalization_wrappe
 from . import _native  # noqa: F401
 
 __all__ = ["BaryTreeInterface", "orthogonalization_wrapper", "interpolation_wrapper", "synthetic",
-           "device", "build"]
+           "device", "autotune", "build"]

@@ -973,11 +973,55 @@ __global__ void __launch_bounds__(FT) pair_peak_far(int reps, float *out) {
     out[blockIdx.x * FT + threadIdx.x] = sum[0] + sum[1] - cmp[0] - cmp[1];
 }
 
+// Yukawa orbital groups: group_tile over one staged tile, 8 orbitals per
+// pair geometry; counted per (pair, orbital).
+template <bool SS>
+__global__ void __launch_bounds__(FT, 2) pair_peak_near_group(int reps, float *out) {
+    constexpr int OG = 8;
+    __shared__ float4 s_xyzw[GTILE];
+    __shared__ float4 s_lo[GTILE];
+    __shared__ float4 s_q4[GTILE * OG / 4];
+    for (int j = threadIdx.x; j < GTILE; j += FT) {
+        const float v = (float)((j * 37) % 101) * 0.01f - 0.5f;
+        s_xyzw[j] = make_float4(v, 0.3f * v + 0.1f, 0.7f - v, 0.25f);
+        s_lo[j] = make_float4(0.f, 0.f, 0.f, 0.f);
+    }
+    for (int k = threadIdx.x; k < GTILE * OG; k += FT) reinterpret_cast<float *>(s_q4)[k] = 0.5f + 0.001f * k;
+    __syncthreads();
+    const float tx = 0.01f * (threadIdx.x & 31), ty = 0.02f, tz = -0.03f * (threadIdx.x >> 5);
+    float fi[OG], kc[OG], kl[OG], sum[OG], cmp[OG];
+#pragma unroll
+    for (int o = 0; o < OG; o++) {
+        fi[o] = 0.3f;
+        split_f32(-(0.5 + 0.3 * o) * LOG2E, kc[o], kl[o]);
+        sum[o] = cmp[o] = 0.f;
+    }
+    for (int r = 0; r < reps; r++)
+        group_tile<SS, false, false, OG>(s_xyzw, s_lo, s_q4, GTILE, tx, ty, tz, 0.f, 0.f, 0.f, fi, kc, kl, sum, cmp);
+    float acc = 0.f;
+#pragma unroll
+    for (int o = 0; o < OG; o++) acc += sum[o] - cmp[o];
+    out[blockIdx.x * FT + threadIdx.x] = acc;
+}
+
+template <int KERN, bool SS>
+int launch_pair_peak(int variant, int grid, int reps, float *out, cudaStream_t s) {
+    if (variant == 0) launch(pair_peak_near<KERN, SS>, grid, FT, 0, s, reps, out);
+    else if (variant == 1) launch(pair_peak_far<KERN, SS>, grid, FT, 0, s, reps, out);
+    else launch(pair_peak_near_group<SS>, grid, FT, 0, s, reps, out);
+    TAGI_LAUNCH_CHECK();
+    return TAGI_OK;
+}
+
 template <int KERN, bool SS>
 int run_pair_peak(int variant, double *pairs_per_s, cudaStream_t s) {
+    if (variant < 0 || variant > 2) return set_error(TAGI_ERR_ARG, "pair peak variant %d (0 near, 1 far, 2 near group)", variant);
+    if (variant == 2 && KERN != KERNEL_YUKAWA)
+        return set_error(TAGI_ERR_UNSUPPORTED, "orbital-group kernels are Yukawa only");
     int grid = 0;
     if (variant == 0) TAGI_TRY(occupancy_grid(pair_peak_near<KERN, SS>, &grid));
-    else TAGI_TRY(occupancy_grid(pair_peak_far<KERN, SS>, &grid));
+    else if (variant == 1) TAGI_TRY(occupancy_grid(pair_peak_far<KERN, SS>, &grid));
+    else TAGI_TRY(occupancy_grid(pair_peak_near_group<SS>, &grid));
     Arena tmp;
     tmp.stream = s;
     float *out = nullptr;
@@ -985,16 +1029,15 @@ int run_pair_peak(int variant, double *pairs_per_s, cudaStream_t s) {
     cudaEvent_t a, b;
     cudaEventCreate(&a);
     cudaEventCreate(&b);
-    const int per_rep = 2 * (variant == 0 ? NTILE : 512);  // two targets per thread
+    // pairs per repetition per thread: two targets x a tile, or one target x a tile x 8 orbitals
+    const int per_rep = variant == 0 ? 2 * NTILE : (variant == 1 ? 2 * 512 : GTILE * 8);
     int reps = 16;
     float ms = 0.f;
     int rc = TAGI_OK;
     for (int attempt = 0; attempt < 6; attempt++) {  // grow until the timed launch lasts >= 20 ms
-        if (variant == 0) launch(pair_peak_near<KERN, SS>, grid, FT, 0, s, reps, out);
-        else launch(pair_peak_far<KERN, SS>, grid, FT, 0, s, reps, out);
+        if ((rc = launch_pair_peak<KERN, SS>(variant, grid, reps, out, s))) break;
         cudaEventRecord(a, s);
-        if (variant == 0) launch(pair_peak_near<KERN, SS>, grid, FT, 0, s, reps, out);
-        else launch(pair_peak_far<KERN, SS>, grid, FT, 0, s, reps, out);
+        if ((rc = launch_pair_peak<KERN, SS>(variant, grid, reps, out, s))) break;
         cudaEventRecord(b, s);
         if (cudaEventSynchronize(b) != cudaSuccess) { rc = set_error(TAGI_ERR_CUDA, "pair peak launch failed"); break; }
         cudaEventElapsedTime(&ms, a, b);
@@ -1300,7 +1343,7 @@ static int orbital_setup(Plan &p, const SysCall &c, int kernel, int singularity,
 // memory: scratch, schedule and FP64 weight charges must exist already, and
 // kernel parameters must be on the device.
 int convolve_systems(SysCall *calls, int nsys, int kernel, int singularity, int precision, const Schedule &sc,
-                     int *queue, cudaStream_t s) {
+                     int *queue, cudaStream_t s, int nt_request) {
     if (nsys < 1 || nsys > MAX_SYSTEMS) return set_error(TAGI_ERR_ARG, "%d systems (1..%d per launch)", nsys, MAX_SYSTEMS);
     const bool mixed = precision == PREC_MIXED;
     const bool ss = singularity == SING_SUBTRACTION;
@@ -1332,12 +1375,13 @@ int convolve_systems(SysCall *calls, int nsys, int kernel, int singularity, int 
         phase_mark(PH_UPWARD, false, s);
         if (!mixed && p.nslots && !p.what64) return set_error(TAGI_ERR_DEVICE, "FP64 weight charges missing");
         f[i] = make_fields(p, c.norb);
-        if (p.max_batch > FT) sh.nt = 2;
+        if (p.max_batch > FT) sh.nt = 2;  // automatic: two targets per thread for batches above FT
         if (p.n1 > sh.maxn1) sh.maxn1 = p.n1;
         // the far and close-range passes write only the batches they visit
         TAGI_CUDA(cudaMemsetAsync(p.far_out, 0, sizeof(double) * (size_t)c.norb * nt, s));
         TAGI_CUDA(cudaMemsetAsync(p.near2_out, 0, sizeof(double) * (size_t)c.norb * nt, s));
     }
+    if (nt_request == 1 || nt_request == 2) sh.nt = nt_request;
     TAGI_CUDA(cudaMemsetAsync(queue, 0, 3 * sizeof(int), s));
     if (kernel == KERNEL_YUKAWA) {
         if (ss) TAGI_TRY((launch_fields<KERNEL_YUKAWA, true>(calls, f, nsys, sc, sh, precision, queue, s)));
@@ -1368,7 +1412,7 @@ int convolve_systems(SysCall *calls, int nsys, int kernel, int singularity, int 
 // work list.
 int convolve(Plan &p, const double *tv, const double *sv, double *out, int norb, int kernel,
              const double *kparams, int nkp, int singularity, int precision, cudaStream_t s, bool kp_device,
-             int og_request) {
+             int og_request, int nt_request) {
     const int og = orbitals_per_item(kernel, precision, norb, og_request);
     const Schedule *sc = nullptr;
     for (const Schedule &c : p.scheds)
@@ -1401,7 +1445,7 @@ int convolve(Plan &p, const double *tv, const double *sv, double *out, int norb,
     c.kp = kparams;
     c.nkp = nkp;
     c.kp_device = kp_device;
-    return convolve_systems(&c, 1, kernel, singularity, precision, *sc, p.queue, s);
+    return convolve_systems(&c, 1, kernel, singularity, precision, *sc, p.queue, s, nt_request);
 }
 
 int pair_peak(int kernel, int singularity, int variant, double kp, double *pairs_per_s, cudaStream_t s) {

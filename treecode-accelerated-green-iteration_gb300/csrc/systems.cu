@@ -20,6 +20,7 @@ struct Systems {
     std::vector<Plan *> plans;  // borrowed
     std::vector<int> norb;
     int kernel = KERNEL_YUKAWA, precision = PREC_MIXED;
+    int nt_request = 0;  // targets per thread: 0 automatic, 1 or 2
     Schedule sched;
     int *queue = nullptr;  // 3 work counters
     cudaStream_t stream = nullptr;
@@ -55,7 +56,7 @@ extern "C" {
 int tagi_plan_convolve_ex(tagi_plan *plan, int numOrbitals, const double *targetValues, const double *sourceValues,
                           double *output, int kernel, int numberOfKernelParameters, const double *kernelParameters,
                           int kernelParametersOnDevice, int singularity, int precision, int orbitalsPerItem,
-                          void *stream) {
+                          int targetsPerThread, void *stream) {
     if (!plan) return set_error(TAGI_ERR_ARG, "null plan");
     Plan &p = *reinterpret_cast<Plan *>(plan);
     if (numOrbitals < 1 || numOrbitals > 0xffff)
@@ -63,6 +64,8 @@ int tagi_plan_convolve_ex(tagi_plan *plan, int numOrbitals, const double *target
     if (!targetValues || !sourceValues || !output) return set_error(TAGI_ERR_ARG, "null device pointer");
     if (orbitalsPerItem != 0 && orbitalsPerItem != 1 && orbitalsPerItem != 4 && orbitalsPerItem != 8)
         return set_error(TAGI_ERR_ARG, "orbitalsPerItem %d must be 0 (automatic), 1, 4 or 8", orbitalsPerItem);
+    if (targetsPerThread < 0 || targetsPerThread > 2)
+        return set_error(TAGI_ERR_ARG, "targetsPerThread %d must be 0 (automatic), 1 or 2", targetsPerThread);
     TAGI_TRY(check_call(kernel, singularity, precision));
     if (kernelParametersOnDevice) {
         if (!kernelParameters || numberOfKernelParameters < 1)
@@ -72,7 +75,7 @@ int tagi_plan_convolve_ex(tagi_plan *plan, int numOrbitals, const double *target
     }
     return convolve(p, targetValues, sourceValues, output, numOrbitals, kernel, kernelParameters,
                     numberOfKernelParameters, singularity, precision, (cudaStream_t)stream,
-                    kernelParametersOnDevice != 0, orbitalsPerItem);
+                    kernelParametersOnDevice != 0, orbitalsPerItem, targetsPerThread);
 }
 
 int tagi_plan_check_parameters(tagi_plan *plan, int *flags, void *stream) {
@@ -86,7 +89,7 @@ int tagi_plan_check_parameters(tagi_plan *plan, int *flags, void *stream) {
 }
 
 int tagi_systems_create(tagi_systems **systems, int numSystems, tagi_plan *const *plans, const int *numOrbitals,
-                        int kernel, int precision, int orbitalsPerItem, void *stream) {
+                        int kernel, int precision, int orbitalsPerItem, int targetsPerThread, void *stream) {
     if (!systems) return set_error(TAGI_ERR_ARG, "null systems pointer");
     *systems = nullptr;
     if (numSystems < 1 || numSystems > MAX_SYSTEMS)
@@ -94,6 +97,8 @@ int tagi_systems_create(tagi_systems **systems, int numSystems, tagi_plan *const
     if (!plans || !numOrbitals) return set_error(TAGI_ERR_ARG, "null plans or numOrbitals");
     if (orbitalsPerItem != 0 && orbitalsPerItem != 1 && orbitalsPerItem != 4 && orbitalsPerItem != 8)
         return set_error(TAGI_ERR_ARG, "orbitalsPerItem %d must be 0 (automatic), 1, 4 or 8", orbitalsPerItem);
+    if (targetsPerThread < 0 || targetsPerThread > 2)
+        return set_error(TAGI_ERR_ARG, "targetsPerThread %d must be 0 (automatic), 1 or 2", targetsPerThread);
     TAGI_TRY(check_call(kernel, SING_SUBTRACTION, precision));
     int maxo = 0;
     for (int i = 0; i < numSystems; i++) {
@@ -106,6 +111,7 @@ int tagi_systems_create(tagi_systems **systems, int numSystems, tagi_plan *const
     y->stream = (cudaStream_t)stream;
     y->kernel = kernel;
     y->precision = precision;
+    y->nt_request = targetsPerThread;
     for (int i = 0; i < numSystems; i++) {
         y->plans.push_back(reinterpret_cast<Plan *>(plans[i]));
         y->norb.push_back(numOrbitals[i]);
@@ -171,7 +177,8 @@ int tagi_systems_convolve(tagi_systems *systems, const double *const *targetValu
         calls[i].nkp = numberOfKernelParameters;
         calls[i].kp_device = kernelParametersOnDevice != 0;
     }
-    return convolve_systems(calls, n, y.kernel, singularity, y.precision, y.sched, y.queue, (cudaStream_t)stream);
+    return convolve_systems(calls, n, y.kernel, singularity, y.precision, y.sched, y.queue, (cudaStream_t)stream,
+                            y.nt_request);
 }
 
 int tagi_systems_destroy(tagi_systems *systems) {
@@ -225,7 +232,7 @@ int tagi_treecode_batched(int numSystems, const int *pointOffsets, const int *nu
             korb += numOrbitals[sid];
         }
         tagi_systems *sys = nullptr;
-        if (!rc) rc = tagi_systems_create(&sys, nc, plans, numOrbitals + c0, kernel, precision, 0, stream);
+        if (!rc) rc = tagi_systems_create(&sys, nc, plans, numOrbitals + c0, kernel, precision, 0, 0, stream);
         if (!rc) rc = tagi_systems_convolve(sys, tv, tv, out, 1, kp, 0, singularity, stream);
         if (!rc && cudaStreamSynchronize(s) != cudaSuccess) rc = set_error(TAGI_ERR_CUDA, "batched convolution failed");
         tagi_systems_destroy(sys);

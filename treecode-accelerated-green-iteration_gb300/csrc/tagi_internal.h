@@ -231,10 +231,10 @@ int orbitals_per_item(int kernel, int precision, int max_norb, int requested);
 int build_schedule(Plan *const *plans, const int *norb, int nsys, int og, Schedule &sc, cudaStream_t s);
 bool schedule_matches(const Schedule &sc, const int *norb, int nsys, int og);
 int convolve_systems(SysCall *calls, int nsys, int kernel, int singularity, int precision,
-                     const Schedule &sc, int *queue, cudaStream_t s);
+                     const Schedule &sc, int *queue, cudaStream_t s, int nt_request = 0);
 int convolve(Plan &p, const double *tv, const double *sv, double *out, int norb, int kernel,
              const double *kparams, int nkp, int singularity, int precision, cudaStream_t s,
-             bool kp_device = false, int og_request = 0);
+             bool kp_device = false, int og_request = 0, int nt_request = 0);
 bool stream_capturing(cudaStream_t s);
 int direct_sum(int nt, const double *tx, const double *ty, const double *tz, const double *tv,
                int nsub, const int *sub, int ns, const double *sx, const double *sy,
