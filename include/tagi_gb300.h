@@ -245,6 +245,54 @@ int tagi_mgs_dev(double *V, double *U, const double *W, int targetWavefunction, 
 int tagi_mgs_dev_noalloc(double *V, double *U, const double *W, int targetWavefunction,
                          int numPoints, int numWavefunctions, void *stream);
 
+/* Green-iteration and SCF steps around the convolution (device pointers,
+ * FP64, no allocation: `work` is a caller workspace of at least
+ * tagi_gi_workspace_doubles(numPoints, rows) doubles).  With these, one
+ * Green-iteration sweep over all orbitals is a sequence of launches that can
+ * be captured as one CUDA graph.  psi, f, conv: [numOrbitals x numPoints]. */
+long long tagi_gi_workspace_doubles(long long numPoints, int rows);
+/* f = -2 psi V_eff (greenIterationFixedPoint.py:155). */
+int tagi_gi_source(const double *psi, const double *veff, long long numPoints, int numOrbitals,
+                   double *f, void *stream);
+/* Harrison update (greenIterationFixedPoint.py:373-399): psi_new = convScale *
+ * conv; dE = -<psi V_eff (psi - psi_new)>_W / <psi_new^2>_W; epsPrev = eps;
+ * eps += dE (an eigenvalue that is not negative is set to gaugeShift - 1.5
+ * and flagged, as :470-477 does with a random offset); k = sqrt(-2 eps);
+ * psi <- psi_new. */
+int tagi_gi_update(double *psi, const double *conv, const double *veff, const double *weights,
+                   long long numPoints, int numOrbitals, double convScale, double *eps,
+                   double *epsPrev, double *k, double gaugeShift, double *deltaE, int *flags,
+                   double *work, long long workDoubles, void *stream);
+/* residual[m] = sqrt(|psi_m - psiPrev_m|_W^2 + (eps_m - epsPrev_m)^2), the
+ * norm of scfFixedPoint.py:62-67; psiResidual[m] without the eigenvalue. */
+int tagi_gi_residual(const double *psi, const double *psiPrev, const double *weights,
+                     long long numPoints, int numOrbitals, const double *eps, const double *epsPrev,
+                     double *residual, double *psiResidual, double *work, long long workDoubles,
+                     void *stream);
+/* out[r] = sum_i w_i a[r][i] b[r][i] (row strides; bStride 0 shares one b;
+ * b NULL: b = 1; weights NULL: w = 1). */
+int tagi_wdot_rows(const double *a, long long aStride, const double *b, long long bStride,
+                   const double *weights, long long numPoints, int rows, double *out, double *work,
+                   long long workDoubles, void *stream);
+/* rho = sum_m occ_m psi_m^2, then scaled so sum_i w_i rho_i = numElectrons
+ * (skipped if numElectrons <= 0) (scfFixedPoint.py:624-636). */
+int tagi_scf_density(const double *psi, const double *occupations, int numOrbitals,
+                     long long numPoints, const double *weights, double numElectrons, double *rho,
+                     double *work, long long workDoubles, void *stream);
+/* Slater exchange, spin-unpolarized LDA: vx = -(3/pi)^(1/3) rho^(1/3), ex
+ * (energy per electron) = 3/4 vx. */
+int tagi_lda_exchange(const double *rho, long long numPoints, double *vx, double *ex, void *stream);
+/* veff = vHartree + vx + vExternal + gaugeShift (scfFixedPoint.py:345). */
+int tagi_veff(const double *vHartree, const double *vx, const double *vExternal, double gaugeShift,
+              long long numPoints, double *veff, void *stream);
+/* Anderson combination (densityMixingSchemes.py:60-97) of ring-buffer
+ * histories [H x numPoints]: newestRow is the latest (in, out) pair,
+ * olderRows[k] the k-th older row, coefficients c_k from the caller's solve of
+ * the weighted linear system; next = b mix_out + (1 - b) mix_in. */
+int tagi_anderson_combine(const double *inHistory, const double *outHistory, int numHistory,
+                          int newestRow, const int *olderRows, const double *coefficients,
+                          double mixingParameter, long long numPoints, double *next, void *stream);
+
 /* Device form of InterpolateBetweenTwoMeshes (TwoMeshInterpolation.c:163);
  * the points-per-cell arrays are device int32 arrays. */
 int tagi_interp_dev(const double *coarseX, const double *coarseY, const double *coarseZ,

@@ -34,9 +34,9 @@ SIGNATURES = {
                               _i, _i, _d, _vp]),
     "tagi_plan_destroy": (_i, [_vp]),
     "tagi_plan_convolve": (_i, [_vp, _i, _vp, _vp, _vp, _i, _i, _dp, _i, _i, _vp]),
-    "tagi_plan_convolve_ex": (_i, [_vp, _i, _vp, _vp, _vp, _i, _i, _vp, _i, _i, _i, _i, _vp]),
+    "tagi_plan_convolve_ex": (_i, [_vp, _i, _vp, _vp, _vp, _i, _i, _vp, _i, _i, _i, _i, _i, _vp]),
     "tagi_plan_check_parameters": (_i, [_vp, _ip, _vp]),
-    "tagi_systems_create": (_i, [ctypes.POINTER(_vp), _i, ctypes.POINTER(_vp), _ip, _i, _i, _i, _vp]),
+    "tagi_systems_create": (_i, [ctypes.POINTER(_vp), _i, ctypes.POINTER(_vp), _ip, _i, _i, _i, _i, _vp]),
     "tagi_systems_convolve": (_i, [_vp, ctypes.POINTER(_vp), ctypes.POINTER(_vp), ctypes.POINTER(_vp), _i,
                                    ctypes.POINTER(_vp), _i, _i, _vp]),
     "tagi_systems_info": (_i, [_vp, _ip]),
@@ -48,6 +48,18 @@ SIGNATURES = {
     "tagi_graph_launch": (_i, [_vp, _vp]),
     "tagi_graph_nodes": (_i, [_vp, _ip]),
     "tagi_graph_destroy": (_i, [_vp]),
+    "tagi_gi_workspace_doubles": (ctypes.c_longlong, [ctypes.c_longlong, _i]),
+    "tagi_gi_source": (_i, [_vp, _vp, ctypes.c_longlong, _i, _vp, _vp]),
+    "tagi_gi_update": (_i, [_vp, _vp, _vp, _vp, ctypes.c_longlong, _i, _d, _vp, _vp, _vp, _d, _vp, _vp, _vp,
+                            ctypes.c_longlong, _vp]),
+    "tagi_gi_residual": (_i, [_vp, _vp, _vp, ctypes.c_longlong, _i, _vp, _vp, _vp, _vp, _vp, ctypes.c_longlong,
+                              _vp]),
+    "tagi_wdot_rows": (_i, [_vp, ctypes.c_longlong, _vp, ctypes.c_longlong, _vp, ctypes.c_longlong, _i, _vp, _vp,
+                            ctypes.c_longlong, _vp]),
+    "tagi_scf_density": (_i, [_vp, _vp, _i, ctypes.c_longlong, _vp, _d, _vp, _vp, ctypes.c_longlong, _vp]),
+    "tagi_lda_exchange": (_i, [_vp, ctypes.c_longlong, _vp, _vp, _vp]),
+    "tagi_veff": (_i, [_vp, _vp, _vp, _d, ctypes.c_longlong, _vp, _vp]),
+    "tagi_anderson_combine": (_i, [_vp, _vp, _i, _i, _vp, _vp, _d, ctypes.c_longlong, _vp, _vp]),
     "tagi_plan_info": (_i, [_vp, _dp]),
     "tagi_plan_get_tree": (_i, [_vp, _i, _u64p, _ip, _ip, _ip, _ip, _ip, _ip, _dp, _dp, _dp]),
     "tagi_plan_get_lists": (_i, [_vp, _ip, _ip, _ip, _ip, _ip, _ip]),

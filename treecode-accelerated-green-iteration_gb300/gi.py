@@ -1,0 +1,129 @@
+"""Green iteration on the device: all orbitals of one mesh per sweep.
+
+One sweep (greenIterationFixedPoint.py:155-484, every orbital at once):
+
+    f_m      = -2 psi_m V_eff
+    c_m      = G_{k_m} * f_m          one batched Yukawa convolution, k_m = sqrt(-2 eps_m)
+    psi_m'   = c_m / (4 pi)
+    eps_m   += -<psi_m V_eff (psi_m - psi_m')>_W / <psi_m'^2>_W
+    psi_m    = psi_m', then Gram-Schmidt in orbital order (Orthogonalization.c:14)
+    residual = |(psi, eps) - (psi, eps)_before|  with weights (W, 1)
+
+The reference iterates one orbital at a time to its tolerance (with Anderson
+mixing on (psi, eps), scfFixedPoint.py:381-597); here every orbital advances
+in the same sweep, so the sweep's convolutions share one launch per field
+pass and the whole sweep is one CUDA graph.  Every buffer is allocated once;
+the sweep's launches never allocate, so ``capture`` records it for replay.
+"""
+import ctypes
+import math
+
+import torch
+
+try:
+    from . import _native
+    from . import device as dev
+    from .BaryTreeInterface import Kernel, Singularity
+except ImportError:
+    import _native
+    import device as dev
+    from BaryTreeInterface import Kernel, Singularity
+
+
+def _p(t):
+    return ctypes.c_void_p(t.data_ptr())
+
+
+class GreenIteration:
+    """Device state and launch sequence of simultaneous Green iteration.
+
+    plan: TreecodePlan over the mesh (targets = sources); weights: [n]
+    quadrature weights; psi: [norb, n] orbitals (updated in place); eps:
+    [norb] eigenvalues; veff: [n] effective potential (the caller may refill
+    it between sweeps, also between graph replays)."""
+
+    def __init__(self, plan, weights, psi, eps, veff, gauge_shift=-0.5, precision="mixed", stream=None):
+        self.plan = plan
+        self.n = int(weights.numel())
+        self.norb = int(psi.shape[0])
+        if psi.shape != (self.norb, self.n):
+            raise ValueError("psi must be [norb, n]")
+        # a created stream of its own by default: graph capture cannot use the default stream
+        self.stream = stream if stream is not None else torch.cuda.Stream()
+        self.stream.wait_stream(torch.cuda.current_stream())
+        self.precision = precision
+        self.gauge = float(gauge_shift)
+        d = psi.device
+        f64 = dict(dtype=torch.float64, device=d)
+        self.w = weights.contiguous()
+        self.psi = psi
+        self.veff = veff
+        self.eps = torch.as_tensor(eps, **f64).contiguous().clone()
+        self.eps_prev = self.eps.clone()
+        self.k = torch.sqrt(-2.0 * self.eps.clamp(max=-1e-12))
+        self.psi_prev = torch.empty_like(psi)
+        self.f = torch.empty_like(psi)
+        self.conv = torch.empty_like(psi)
+        self.dE = torch.zeros(self.norb, **f64)
+        self.flags = torch.zeros(self.norb, dtype=torch.int32, device=d)
+        self.res = torch.zeros(self.norb, **f64)
+        self.psi_res = torch.zeros(self.norb, **f64)
+        L = _native.lib()
+        nw = int(L.tagi_gi_workspace_doubles(self.n, self.norb))
+        self.work = torch.empty(nw, **f64)
+        self._graph = None
+
+    def set_eigenvalues(self, eps):
+        self.eps.copy_(torch.as_tensor(eps, dtype=torch.float64))
+        self.k.copy_(torch.sqrt(-2.0 * self.eps.clamp(max=-1e-12)))
+
+    def _launches(self):
+        L = _native.lib()
+        s = ctypes.c_void_p(self.stream.cuda_stream)
+        n, m = self.n, self.norb
+        self.psi_prev.copy_(self.psi)
+        _native.check(L.tagi_gi_source(_p(self.psi), _p(self.veff), n, m, _p(self.f), s))
+        self.plan.convolve(self.f, self.f, Kernel.YUKAWA, self.k, Singularity.SUBTRACTION,
+                           precision=self.precision, out=self.conv, stream=self.stream)
+        _native.check(L.tagi_gi_update(_p(self.psi), _p(self.conv), _p(self.veff), _p(self.w), n, m,
+                                       1.0 / (4.0 * math.pi), _p(self.eps), _p(self.eps_prev), _p(self.k),
+                                       self.gauge, _p(self.dE), _p(self.flags), _p(self.work),
+                                       self.work.numel(), s))
+        for j in range(m):
+            row = self.psi[j]
+            _native.check(L.tagi_mgs_dev_noalloc(_p(self.psi), _p(row), _p(self.w), j, n, m, s))
+        _native.check(L.tagi_gi_residual(_p(self.psi), _p(self.psi_prev), _p(self.w), n, m, _p(self.eps),
+                                         _p(self.eps_prev), _p(self.res), _p(self.psi_res), _p(self.work),
+                                         self.work.numel(), s))
+
+    def sweep(self):
+        """One sweep, launched eagerly on the stream."""
+        with torch.cuda.stream(self.stream):
+            self._launches()
+
+    def capture(self):
+        """Record one sweep as a CUDA graph (after at least one eager sweep)."""
+        if self._graph is not None:
+            self._graph.close()
+        with torch.cuda.stream(self.stream):
+            with dev.Graph.capture(self.stream) as g:
+                self._launches()
+        self._graph = g
+        return g
+
+    def replay(self):
+        if self._graph is None:
+            raise RuntimeError("capture() first")
+        self._graph.replay(self.stream)
+
+    def step(self):
+        """One sweep: graph replay when captured, else eager."""
+        if self._graph is not None:
+            self.replay()
+        else:
+            self.sweep()
+
+    def close(self):
+        if self._graph is not None:
+            self._graph.close()
+            self._graph = None
