@@ -293,6 +293,49 @@ int tagi_anderson_combine(const double *inHistory, const double *outHistory, int
                           int newestRow, const int *olderRows, const double *coefficients,
                           double mixingParameter, long long numPoints, double *next, void *stream);
 
+/* Learned extrapolation network (no counterpart in the reference): kernels
+ * for a 3-layer MLP on per-cell patches with BF16 weights and FP32
+ * accumulation, trained on the device.  BF16 arrays are passed as void*. */
+/* C[M x N] = A[M x K] B[K x N] on the tensor cores; element (m, k) of A is
+ * A[m sAm + k sAk], (k, n) of B is B[k sBk + n sBn].  epilogue 0: f32 C32;
+ * 1: bf16 C16 = relu(C + bias); 2: bf16 C16 = C * (mask > 0) (mask bf16,
+ * same layout as C); 3: f32 C32 = C + bias.  ldc: row stride of C. */
+int tagi_mlp_gemm(const void *A, long long sAm, long long sAk, const void *B, long long sBk,
+                  long long sBn, int M, int N, int K, int epilogue, float *C32, void *C16,
+                  long long ldc, const float *bias, const void *mask, void *stream);
+/* f32 C = A B with K split over up to `splits` blocks (partial holds splits *
+ * M * N floats); the partials are added in a fixed order. */
+int tagi_mlp_gemm_splitk(const void *A, long long sAm, long long sAk, const void *B, long long sBk,
+                         long long sBn, int M, int N, int K, int splits, float *partial, float *C,
+                         void *stream);
+/* Rows (orbital, cell) of features [psi/s_psi, d/s_d, eps, 0...] (bf16, row
+ * stride ldx >= 2P+1), the patch scales s_d (floored by dfloor[orbital]) and
+ * d/s_d in f32.  The mesh stores each cell's P points contiguously. */
+int tagi_mlp_patch_features(const double *psi, const double *d, const double *eps,
+                            const double *dfloor, int numOrbitals, int numCells, int P,
+                            long long numPoints, int ldx, void *X, float *scale, float *dn,
+                            void *stream);
+/* T = dnext / s_d per row. */
+int tagi_mlp_patch_target(const double *dnext, const float *scale, int numOrbitals, int numCells,
+                          int P, long long numPoints, float *T, void *stream);
+/* r = alpha dn + Y - T; lossAndDalpha = {sum r^2, sum dY dn}; dY = 2r/(rows P)
+ * in f32 and bf16; part: 2*rows floats. */
+int tagi_mlp_mse_grad(const float *Y, const float *dn, const float *T, const float *alpha, int rows,
+                      int P, float *dY, void *dY16, float *part, float *lossAndDalpha, void *stream);
+long long tagi_mlp_colsum_workspace(long long rows, int N);
+/* Column sums of a [rows x N] f32 (isBf16 = 0) or bf16 matrix. */
+int tagi_mlp_colsum(const void *G, int isBf16, long long rows, int N, float *out, float *work,
+                    long long workFloats, void *stream);
+/* One Adam step on FP32 weights (bias-corrected with `step`); w16 (optional)
+ * receives the BF16 copy. */
+int tagi_mlp_adam(float *w, const float *g, float *m1, float *m2, long long n, float lr, float beta1,
+                  float beta2, float epsilon, int step, void *w16, void *stream);
+/* psiOut = psi + s_d (alpha dn + Y) per patch, dOut = the increment (may alias). */
+int tagi_mlp_patch_apply(const double *psi, const float *Y, const float *dn, const float *scale,
+                         const float *alpha, int numOrbitals, int numCells, int P,
+                         long long numPoints, double *psiOut, double *dOut, void *stream);
+int tagi_mlp_to_bf16(const float *a, long long n, void *b, void *stream);
+
 /* Device form of InterpolateBetweenTwoMeshes (TwoMeshInterpolation.c:163);
  * the points-per-cell arrays are device int32 arrays. */
 int tagi_interp_dev(const double *coarseX, const double *coarseY, const double *coarseZ,

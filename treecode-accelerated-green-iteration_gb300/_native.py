@@ -60,6 +60,19 @@ SIGNATURES = {
     "tagi_lda_exchange": (_i, [_vp, ctypes.c_longlong, _vp, _vp, _vp]),
     "tagi_veff": (_i, [_vp, _vp, _vp, _d, ctypes.c_longlong, _vp, _vp]),
     "tagi_anderson_combine": (_i, [_vp, _vp, _i, _i, _vp, _vp, _d, ctypes.c_longlong, _vp, _vp]),
+    "tagi_mlp_gemm": (_i, [_vp, ctypes.c_longlong, ctypes.c_longlong, _vp, ctypes.c_longlong, ctypes.c_longlong,
+                           _i, _i, _i, _i, _vp, _vp, ctypes.c_longlong, _vp, _vp, _vp]),
+    "tagi_mlp_gemm_splitk": (_i, [_vp, ctypes.c_longlong, ctypes.c_longlong, _vp, ctypes.c_longlong,
+                                  ctypes.c_longlong, _i, _i, _i, _i, _vp, _vp, _vp]),
+    "tagi_mlp_patch_features": (_i, [_vp, _vp, _vp, _vp, _i, _i, _i, ctypes.c_longlong, _i, _vp, _vp, _vp, _vp]),
+    "tagi_mlp_patch_target": (_i, [_vp, _vp, _i, _i, _i, ctypes.c_longlong, _vp, _vp]),
+    "tagi_mlp_mse_grad": (_i, [_vp, _vp, _vp, _vp, _i, _i, _vp, _vp, _vp, _vp, _vp]),
+    "tagi_mlp_colsum_workspace": (ctypes.c_longlong, [ctypes.c_longlong, _i]),
+    "tagi_mlp_colsum": (_i, [_vp, _i, ctypes.c_longlong, _i, _vp, _vp, ctypes.c_longlong, _vp]),
+    "tagi_mlp_adam": (_i, [_vp, _vp, _vp, _vp, ctypes.c_longlong, ctypes.c_float, ctypes.c_float, ctypes.c_float,
+                           ctypes.c_float, _i, _vp, _vp]),
+    "tagi_mlp_patch_apply": (_i, [_vp, _vp, _vp, _vp, _vp, _i, _i, _i, ctypes.c_longlong, _vp, _vp, _vp]),
+    "tagi_mlp_to_bf16": (_i, [_vp, ctypes.c_longlong, _vp, _vp]),
     "tagi_plan_info": (_i, [_vp, _dp]),
     "tagi_plan_get_tree": (_i, [_vp, _i, _u64p, _ip, _ip, _ip, _ip, _ip, _ip, _dp, _dp, _dp]),
     "tagi_plan_get_lists": (_i, [_vp, _ip, _ip, _ip, _ip, _ip, _ip]),

@@ -215,6 +215,8 @@ class SCF:
     def green_iterations(self, tol, max_sweeps, min_sweeps=1):
         """Sweeps until the largest orbital residual (with eigenvalue) is below tol."""
         sweeps, res = 0, float("inf")
+        if self.extrapolator is not None:
+            self.extrapolator.reset()  # a new potential: earlier iterates no longer predict this one
         while sweeps < max_sweeps:
             if self.extrapolator is not None:
                 res = self.extrapolator.sweep(self)
