@@ -75,6 +75,22 @@ def dist_env():
     return ws, rank, local
 
 
+def job_time_ms(local_ms, device=None):
+    """Whole-job time: the slowest rank's timed region (MAX all-reduce; one rank: itself)."""
+    import torch
+    import torch.distributed as dist
+    if not (dist.is_available() and dist.is_initialized()) or dist.get_world_size() == 1:
+        return float(local_ms)
+    t = torch.tensor([float(local_ms)], dtype=torch.float64, device=device)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def job_value(units_per_rank_step, steps, world_size, total_ms):
+    """Throughput of the whole job: units all ranks processed / the job time."""
+    return units_per_rank_step * steps * world_size / (total_ms * 1e-3)
+
+
 # ---------------------------------------------------------------------------
 # Workloads
 # ---------------------------------------------------------------------------
@@ -311,13 +327,8 @@ def gb300_arm(args):
     L.tagi_profile_read(nat.dptr(prof_ms), prof_np, 7)
     L.tagi_profile(0)
     step_ms = [a.elapsed_time(b) for a, b in evs]
-    total_ms = float(sum(step_ms))
-    if ws > 1:
-        tt = torch.tensor([total_ms], device=cuda)
-        dist.all_reduce(tt, op=dist.ReduceOp.MAX)
-        total_ms = float(tt.item())
-    convs = norb * args.steps * ws
-    value = convs / (total_ms * 1e-3)
+    total_ms = job_time_ms(float(sum(step_ms)), cuda)
+    value = job_value(norb, args.steps, ws, total_ms)
 
     if rank != 0:
         if ws > 1:
@@ -491,13 +502,9 @@ def uneven_arm(args):
     # launches inside the timed region: every replay runs the captured kernels
     launches_per_replay = None
     step_ms = [a.elapsed_time(b) for a, b in evs]
-    total_ms = float(sum(step_ms))
-    if ws > 1:
-        tt = torch.tensor([total_ms], device=cuda)
-        dist.all_reduce(tt, op=dist.ReduceOp.MAX)
-        total_ms = float(tt.item())
+    total_ms = job_time_ms(float(sum(step_ms)), cuda)
     orb_total = sum(norbs)
-    value = orb_total * args.steps * ws / (total_ms * 1e-3)
+    value = job_value(orb_total, args.steps, ws, total_ms)
     if rank != 0:
         if ws > 1:
             dist.destroy_process_group()
