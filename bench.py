@@ -59,7 +59,10 @@ def parse():
     ap.add_argument("--steps", type=int, default=5)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
-    ap.add_argument("--workload", default="hartree", choices=["hartree", "orbitals", "uneven"])
+    ap.add_argument("--workload", default="hartree", choices=["hartree", "orbitals", "uneven", "scf"])
+    ap.add_argument("--scf-points", type=int, default=3_000_000, help="scf workload: mesh points")
+    ap.add_argument("--scf-max-iter", type=int, default=60)
+    ap.add_argument("--scf-time-limit", type=float, default=1500.0, help="scf workload: seconds per run")
     ap.add_argument("--fp64-sample-systems", type=int, default=2,
                     help="uneven workload: systems whose plain FP64 one-call-per-orbital time is measured")
     ap.add_argument("--cpu-seconds", type=float, default=15.0,
@@ -644,12 +647,93 @@ def uneven_arm(args):
     return 0
 
 
+# ---------------------------------------------------------------------------
+# Ring-molecule SCF: plain Green iteration vs the learned extrapolation
+# ---------------------------------------------------------------------------
+def ring_guess(mesh, nuclei, charges, norb=21):
+    """Atom-centred start: carbon 1s, carbon 2s, hydrogen 1s, carbon 2p_z; eigenvalue guesses."""
+    funcs, eps = [], []
+    for kind in ("c1s", "c2s", "h1s", "c2pz"):
+        for R, z in zip(nuclei, charges):
+            dx, dy, dz = mesh.x - R[0], mesh.y - R[1], mesh.z - R[2]
+            r = np.sqrt(dx * dx + dy * dy + dz * dz)
+            if kind == "c1s" and z > 1:
+                funcs.append(np.exp(-5.7 * r))
+                eps.append(-10.0)
+            elif kind == "c2s" and z > 1:
+                funcs.append((1 - 0.8 * r) * np.exp(-1.6 * r))
+                eps.append(-0.7)
+            elif kind == "h1s" and z == 1:
+                funcs.append(np.exp(-r))
+                eps.append(-0.5)
+            elif kind == "c2pz" and z > 1:
+                funcs.append(dz * np.exp(-1.6 * r))
+                eps.append(-0.4)
+    return np.stack(funcs[:norb]), np.array(eps[:norb])
+
+
+def scf_arm(args):
+    import torch
+    ws, rank, local = dist_env()
+    torch.cuda.set_device(local)
+    if rank != 0:
+        return 0
+    pkg = importlib.import_module(PKG)
+    scf_mod = importlib.import_module(PKG + ".scf")
+    learned = importlib.import_module(PKG + ".learned")
+    L = pkg._native.lib()
+    nuclei, charges = pkg.synthetic.ring_molecule()
+    t0 = time.perf_counter()
+    mesh = pkg.synthetic.mesh_with_points(nuclei, charges, 7, 8, args.scf_points)
+    mesh_s = time.perf_counter() - t0
+    psi0, eps0 = ring_guess(mesh, nuclei, charges)
+    gauge = -0.5
+    runs = {}
+    for name in ("plain", "learned"):
+        ex = learned.LearnedExtrapolator(512, rollout=8) if name == "learned" else None
+        torch.cuda.synchronize()
+        n0 = L.tagi_launch_count()
+        with ClockSampler(local) as clocks:
+            a = time.perf_counter()
+            s = scf_mod.SCF(mesh.x, mesh.y, mesh.z, mesh.w, nuclei, charges, psi0, eps0 + gauge, 42.0,
+                            gauge_shift=gauge, source_leaf=2000, target_leaf=2000, extrapolator=ex)
+            out = s.run(tol=1e-5, max_scf=args.scf_max_iter, time_limit=args.scf_time_limit)
+            wall = time.perf_counter() - a
+        runs[name] = dict(converged=out["converged"], seconds=wall, scf_iterations=out["iterations"],
+                          sweeps=(ex.stats["sweeps"] if ex else out["sweeps"]), Etotal=out["Etotal"],
+                          eigenvalues=out["eigenvalues"], launches=int(L.tagi_launch_count() - n0),
+                          last_eigenvalue_change=s.history[-1]["eigenvalue_change"],
+                          learned_stats=(dict(ex.stats, disabled=ex.disabled) if ex else None),
+                          clocks=clocks.summary())
+        s.close()
+        del s
+        torch.cuda.empty_cache()
+    pl, le = runs["plain"], runs["learned"]
+    line = {
+        "metric": METRIC, "value": le["seconds"], "unit": "s to 1e-5 Ha eigenvalue change (learned)",
+        "n_gpus": 1, "steps": 1, "warmup": 0, "ms_per_step": le["seconds"] * 1e3, "higher_is_better": False,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f32+f64",
+        "data": "synthetic ring molecule (6 C at r=2.6, 6 H at r=4.7 Bohr), seeded mesh",
+        "config": {"workload": "ring_scf_21_orbitals", "points": int(mesh.n), "orbitals": 21, "electrons": 42,
+                   "theta": THETA, "degree": DEGREE, "leaf": [2000, 2000], "precision": "mixed",
+                   "exchange": "Slater (LDA, no correlation)", "orbital_mixing": "Anderson, history 5",
+                   "density_mixing": "Anderson, history 10, beta 0.5", "mesh_build_s": mesh_s,
+                   "step": "one full SCF run from the atom-centred guess"},
+        "plain": pl, "learned": le, "speedup_learned_vs_plain": pl["seconds"] / le["seconds"],
+        "clocks": le["clocks"], "gpu_launches": le["launches"],
+    }
+    print(json.dumps(line), flush=True)
+    return 0
+
+
 def main():
     args = parse()
     if args.impl == "reference":
         return reference_arm(args)
     if args.workload == "uneven":
         return uneven_arm(args)
+    if args.workload == "scf":
+        return scf_arm(args)
     return gb300_arm(args)
 
 

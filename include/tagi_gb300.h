@@ -269,6 +269,22 @@ int tagi_gi_residual(const double *psi, const double *psiPrev, const double *wei
                      long long numPoints, int numOrbitals, const double *eps, const double *epsPrev,
                      double *residual, double *psiResidual, double *work, long long workDoubles,
                      void *stream);
+/* Anderson mixing of every orbital's (psi, eps) over its last numHistory
+ * sweeps (<= 8), the orbital-wise mixing of scfFixedPoint.py:483-597 done for
+ * all orbitals at once.  F = out - in rows, layout [H x numOrbitals x numPoints].
+ * gram[m][q] = sum_i w_i F_a[m][i] F_b[m][i] for the pairs a <= b of rows
+ * 0..numHistory-1 in row-major order (q = a H - a(a-1)/2 + b - a); the caller
+ * adds the eigenvalue parts and solves the small systems.  work: at least
+ * tagi_gi_anderson_workspace_doubles doubles. */
+long long tagi_gi_anderson_workspace_doubles(long long numPoints, int numHistory, int numOrbitals);
+int tagi_gi_anderson_gram(const double *F, int numHistory, int numOrbitals, long long numPoints,
+                          const double *weights, double *gram, double *work, long long workDoubles,
+                          void *stream);
+/* psi[m] = x_l + sum_k c_mk (x_k - x_l) + b (F_l + sum_k c_mk (F_k - F_l)) with
+ * X the input rows, l = newestRow, k over olderRows, c [numOrbitals x (H-1)]. */
+int tagi_gi_anderson_mix(const double *X, const double *F, int numHistory, int newestRow,
+                         const int *olderRows, const double *coefficients, double mixingParameter,
+                         int numOrbitals, long long numPoints, double *psi, void *stream);
 /* out[r] = sum_i w_i a[r][i] b[r][i] (row strides; bStride 0 shares one b;
  * b NULL: b = 1; weights NULL: w = 1). */
 int tagi_wdot_rows(const double *a, long long aStride, const double *b, long long bStride,

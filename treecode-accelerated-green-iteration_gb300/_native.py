@@ -73,6 +73,9 @@ SIGNATURES = {
                            ctypes.c_float, _i, _vp, _vp]),
     "tagi_mlp_patch_apply": (_i, [_vp, _vp, _vp, _vp, _vp, _i, _i, _i, ctypes.c_longlong, _vp, _vp, _vp]),
     "tagi_mlp_to_bf16": (_i, [_vp, ctypes.c_longlong, _vp, _vp]),
+    "tagi_gi_anderson_workspace_doubles": (ctypes.c_longlong, [ctypes.c_longlong, _i, _i]),
+    "tagi_gi_anderson_gram": (_i, [_vp, _i, _i, ctypes.c_longlong, _vp, _vp, _vp, ctypes.c_longlong, _vp]),
+    "tagi_gi_anderson_mix": (_i, [_vp, _vp, _i, _i, _vp, _vp, _d, _i, ctypes.c_longlong, _vp, _vp]),
     "tagi_plan_info": (_i, [_vp, _dp]),
     "tagi_plan_get_tree": (_i, [_vp, _i, _u64p, _ip, _ip, _ip, _ip, _ip, _ip, _dp, _dp, _dp]),
     "tagi_plan_get_lists": (_i, [_vp, _ip, _ip, _ip, _ip, _ip, _ip]),

@@ -226,6 +226,76 @@ __global__ void anderson_combine(const double *__restrict__ in_hist, const doubl
     next[i] = beta * mo + (1.0 - beta) * mi;
 }
 
+// Anderson mixing of each orbital's (psi, eps) over its last H sweeps
+// (scfFixedPoint.py:483-597 does it orbital by orbital; here all orbitals at
+// once).  F = out - in rows, layout [H][norb][n].  Gram partials of every
+// pair a <= b of history rows, per orbital and chunk, in a fixed order.
+constexpr int AND_MAXH = 8;
+
+__global__ void __launch_bounds__(GT) anderson_gram_partial(const double *__restrict__ F, int H, int norb, long n,
+                                                            const double *__restrict__ w, long chunk, int nblk,
+                                                            double *__restrict__ part) {
+    __shared__ double sh[GT / 32];
+    const int m = blockIdx.y;
+    const long j0 = (long)blockIdx.x * chunk, j1 = min(j0 + chunk, n);
+    constexpr int NP = AND_MAXH * (AND_MAXH + 1) / 2;
+    double acc[NP];
+#pragma unroll
+    for (int p = 0; p < NP; p++) acc[p] = 0.0;
+    for (long j = j0 + threadIdx.x; j < j1; j += GT) {
+        double f[AND_MAXH];
+#pragma unroll
+        for (int a = 0; a < AND_MAXH; a++) f[a] = a < H ? F[((long)a * norb + m) * n + j] : 0.0;
+        const double wj = w[j];
+        int p = 0;
+#pragma unroll
+        for (int a = 0; a < AND_MAXH; a++)
+#pragma unroll
+            for (int b = a; b < AND_MAXH; b++) acc[p++] += wj * f[a] * f[b];
+    }
+    const int np = H * (H + 1) / 2;
+    int p = 0;
+#pragma unroll
+    for (int a = 0; a < AND_MAXH; a++)
+#pragma unroll
+        for (int b = a; b < AND_MAXH; b++, p++) {
+            if (a >= H || b >= H) continue;
+            const double t = block_sum(acc[p], sh);
+            // pair index among the first H rows, in the same (a, b) order
+            const int q = a * H - a * (a - 1) / 2 + (b - a);
+            if (threadIdx.x == 0) part[((long)m * nblk + blockIdx.x) * np + q] = t;
+        }
+}
+
+__global__ void anderson_gram_final(const double *__restrict__ part, int nblk, int norb, int np,
+                                    double *__restrict__ gram) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= norb * np) return;
+    const int m = i / np, q = i - m * np;
+    double s = 0.0;
+    for (int b = 0; b < nblk; b++) s += part[((long)m * nblk + b) * np + q];
+    gram[i] = s;
+}
+
+// psi[m] = x_l + sum_k c_mk (x_k - x_l) + beta (F_l + sum_k c_mk (F_k - F_l))
+__global__ void anderson_mix(const double *__restrict__ X, const double *__restrict__ F, int nh, int last,
+                             const int *__restrict__ rows, const double *__restrict__ c, double beta, int norb,
+                             long n, double *__restrict__ psi) {
+    const long i = (long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    const int m = blockIdx.y;
+    const long ol = ((long)last * norb + m) * n + i;
+    const double xl = X[ol], fl = F[ol];
+    double xm = xl, fm = fl;
+    for (int k = 0; k < nh - 1; k++) {
+        const long o = ((long)rows[k] * norb + m) * n + i;
+        const double ck = c[(long)m * (nh - 1) + k];
+        xm += ck * (X[o] - xl);
+        fm += ck * (F[o] - fl);
+    }
+    psi[(long)m * n + i] = xm + beta * fm;
+}
+
 }  // namespace
 
 }  // namespace tagi
@@ -314,6 +384,41 @@ int tagi_scf_density(const double *psi, const double *occupations, int numOrbita
         TAGI_TRY(tagi_wdot_rows(rho, 0, nullptr, 0, weights, numPoints, 1, integral, work, workDoubles - 1, stream));
         launch(scale_to, g, 256, 0, s, rho, (long)numPoints, numElectrons, integral);
     }
+    TAGI_LAUNCH_CHECK();
+    return TAGI_OK;
+}
+
+long long tagi_gi_anderson_workspace_doubles(long long numPoints, int numHistory, int numOrbitals) {
+    const Chunks c = chunks_for(numPoints > 0 ? numPoints : 1);
+    return (long long)c.nblk * numOrbitals * (numHistory * (numHistory + 1) / 2);
+}
+
+int tagi_gi_anderson_gram(const double *F, int numHistory, int numOrbitals, long long numPoints,
+                          const double *weights, double *gram, double *work, long long workDoubles, void *stream) {
+    if (!F || !weights || !gram || !work) return set_error(TAGI_ERR_ARG, "null pointer");
+    if (numHistory < 1 || numHistory > AND_MAXH)
+        return set_error(TAGI_ERR_ARG, "history %d outside [1, %d]", numHistory, AND_MAXH);
+    if (numPoints <= 0 || numOrbitals <= 0 || numOrbitals > 65535) return set_error(TAGI_ERR_ARG, "bad sizes");
+    const Chunks c = chunks_for(numPoints);
+    const int np = numHistory * (numHistory + 1) / 2;
+    if (workDoubles < (long long)c.nblk * numOrbitals * np) return set_error(TAGI_ERR_ARG, "workspace too small");
+    cudaStream_t s = (cudaStream_t)stream;
+    launch(anderson_gram_partial, dim3(c.nblk, numOrbitals), GT, 0, s, F, numHistory, numOrbitals, (long)numPoints,
+           weights, c.chunk, c.nblk, work);
+    launch(anderson_gram_final, (numOrbitals * np + 127) / 128, 128, 0, s, work, c.nblk, numOrbitals, np, gram);
+    TAGI_LAUNCH_CHECK();
+    return TAGI_OK;
+}
+
+int tagi_gi_anderson_mix(const double *X, const double *F, int numHistory, int newestRow, const int *olderRows,
+                         const double *coefficients, double mixingParameter, int numOrbitals, long long numPoints,
+                         double *psi, void *stream) {
+    if (!X || !F || !psi || (numHistory > 1 && (!olderRows || !coefficients)))
+        return set_error(TAGI_ERR_ARG, "null pointer");
+    if (numHistory < 1 || numHistory > AND_MAXH || numPoints <= 0 || numOrbitals <= 0 || numOrbitals > 65535)
+        return set_error(TAGI_ERR_ARG, "bad sizes");
+    launch(anderson_mix, dim3((unsigned)((numPoints + 255) / 256), numOrbitals), 256, 0, (cudaStream_t)stream, X, F,
+           numHistory, newestRow, olderRows, coefficients, mixingParameter, numOrbitals, (long)numPoints, psi);
     TAGI_LAUNCH_CHECK();
     return TAGI_OK;
 }

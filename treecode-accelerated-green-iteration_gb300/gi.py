@@ -18,6 +18,7 @@ the sweep's launches never allocate, so ``capture`` records it for replay.
 import ctypes
 import math
 
+import numpy as np
 import torch
 
 try:
@@ -72,6 +73,7 @@ class GreenIteration:
         nw = int(L.tagi_gi_workspace_doubles(self.n, self.norb))
         self.work = torch.empty(nw, **f64)
         self._graph = None
+        self.anderson = None
 
     def set_eigenvalues(self, eps):
         self.eps.copy_(torch.as_tensor(eps, dtype=torch.float64))
@@ -122,6 +124,82 @@ class GreenIteration:
             self.replay()
         else:
             self.sweep()
+
+    # -- Anderson mixing of (psi, eps) per orbital (scfFixedPoint.py:483-597) ----------
+    def enable_anderson(self, history=5, mixing=0.5, activate=3e-2):
+        """After every sweep once the largest residual is below `activate`, mix
+        each orbital's (psi, eps) over its last `history` sweeps (weights (W, 1)),
+        then Gram-Schmidt: the mixed orbitals are the next sweep's input."""
+        H = int(history)
+        if not 2 <= H <= 8:
+            raise ValueError("history must be in [2, 8]")
+        f64 = dict(dtype=torch.float64, device=self.psi.device)
+        L = _native.lib()
+        self.anderson = dict(H=H, beta=float(mixing), activate=float(activate), count=0,
+                             X=torch.zeros(H, self.norb, self.n, **f64),
+                             F=torch.zeros(H, self.norb, self.n, **f64),
+                             ex=np.zeros((H, self.norb)), ef=np.zeros((H, self.norb)),
+                             gram=torch.zeros(self.norb * H * (H + 1) // 2, **f64),
+                             work=torch.empty(int(L.tagi_gi_anderson_workspace_doubles(self.n, H, self.norb)),
+                                              **f64),
+                             mixed=0)
+
+    def reset_anderson(self):
+        if self.anderson is not None:
+            self.anderson["count"] = 0
+
+    def anderson_step(self, residual):
+        """Mix after a sweep (the stream must be idle); returns True if it mixed."""
+        a = self.anderson
+        if a is None or (a["count"] == 0 and residual > a["activate"]):
+            return False
+        H, m, n = a["H"], self.norb, self.n
+        row = a["count"] % H
+        with torch.cuda.stream(self.stream):
+            a["X"][row].copy_(self.psi_prev)
+            torch.sub(self.psi, self.psi_prev, out=a["F"][row])
+            e_in, e_out = self.eps_prev.cpu().numpy(), self.eps.cpu().numpy()
+            a["ex"][row], a["ef"][row] = e_in, e_out - e_in
+            a["count"] += 1
+            nh = min(a["count"], H)
+            if nh < 2:
+                return False
+            L = _native.lib()
+            s = ctypes.c_void_p(self.stream.cuda_stream)
+            _native.check(L.tagi_gi_anderson_gram(_p(a["F"]), nh, m, n, _p(self.w), _p(a["gram"]), _p(a["work"]),
+                                                  a["work"].numel(), s))
+            np_ = nh * (nh + 1) // 2
+            G = a["gram"][: m * np_].cpu().numpy().reshape(m, np_)
+
+            def idx(i, j):
+                i, j = min(i, j), max(i, j)
+                return i * nh - i * (i - 1) // 2 + (j - i)
+
+            older = [(row - 1 - k) % H for k in range(nh - 1)]
+            c = np.zeros((m, nh - 1))
+            eps_new = np.empty(m)
+            for o in range(m):
+                g = lambda i, j: G[o, idx(i, j)] + a["ef"][i, o] * a["ef"][j, o]
+                A = np.array([[g(row, row) - g(row, ki) - g(row, kj) + g(ki, kj) for kj in older] for ki in older])
+                rhs = np.array([g(row, row) - g(row, ki) for ki in older])
+                try:
+                    c[o] = np.linalg.solve(A, rhs)
+                except np.linalg.LinAlgError:
+                    c[o] = np.linalg.lstsq(A, rhs, rcond=None)[0]
+                xm = a["ex"][row, o] + sum(c[o, k] * (a["ex"][ki, o] - a["ex"][row, o]) for k, ki in enumerate(older))
+                fm = a["ef"][row, o] + sum(c[o, k] * (a["ef"][ki, o] - a["ef"][row, o]) for k, ki in enumerate(older))
+                e = xm + a["beta"] * fm
+                eps_new[o] = e if e < 0.0 else self.gauge - 1.5
+            rows_t = torch.as_tensor(np.asarray(older, dtype=np.int32), device=self.psi.device)
+            c_t = torch.as_tensor(c, dtype=torch.float64, device=self.psi.device).contiguous()
+            _native.check(L.tagi_gi_anderson_mix(_p(a["X"]), _p(a["F"]), nh, row, _p(rows_t), _p(c_t), a["beta"], m,
+                                                 n, _p(self.psi), s))
+            for j in range(m):  # the mixed orbitals are no longer orthonormal
+                _native.check(L.tagi_mgs_dev_noalloc(_p(self.psi), _p(self.psi[j]), _p(self.w), j, n, m, s))
+            self.set_eigenvalues(eps_new)
+            self.stream.synchronize()
+        a["mixed"] += 1
+        return True
 
     def close(self):
         if self._graph is not None:

@@ -155,6 +155,7 @@ class LearnedExtrapolator:
         self.warmup, self.cooldown_len, self.floor = int(warmup), int(cooldown), float(floor)
         self.hidden, self.lr, self.seed = hidden, lr, seed
         self.net = None
+        self.disabled = False  # set for the rest of the run when too few jumps are kept
         self.gate = None  # running ratio of validation losses: full network / skip term alone
         self.stats = dict(proposals=0, accepted=0, rejected=0, trained=0, sweeps=0, extra_sweeps=0)
         self.reset()
@@ -221,6 +222,8 @@ class LearnedExtrapolator:
         """psi <- psi_t + sum of `rollout` predicted updates, Gram-Schmidt'ed; backup kept."""
         L = _native.lib()
         s = ctypes.c_void_p(gi.stream.cuda_stream)
+        if hasattr(gi, "reset_anderson"):
+            gi.reset_anderson()  # a jump breaks the sweep history that orbital mixing works on
         self.backup_psi.copy_(gi.psi)
         self.backup_eps.copy_(gi.eps)
         self.work_psi.copy_(gi.psi)
@@ -274,6 +277,8 @@ class LearnedExtrapolator:
                 self.stats["extra_sweeps"] += 1
                 gi.psi.copy_(self.backup_psi)
                 gi.set_eigenvalues(self.backup_eps.cpu().numpy())
+                if hasattr(gi, "reset_anderson"):
+                    gi.reset_anderson()
                 self.cool = self.backoff
                 self.backoff = min(2 * self.backoff + 1, 16)
                 scf._gi_sweep()
@@ -288,7 +293,13 @@ class LearnedExtrapolator:
             self.last_res = res
             if len(self.hist) == 3:
                 self._train(gi)
-                if self.stats["trained"] >= self.warmup and self.cool == 0 and res > self.min_residual:
+                # the plain method judges the learner as a whole too: a run in which fewer
+                # than a third of the jumps survive stops proposing
+                p = self.stats["proposals"]
+                if p >= 6 and self.stats["accepted"] * 3 < p:
+                    self.disabled = True
+                if (not self.disabled and self.stats["trained"] >= self.warmup and self.cool == 0
+                        and res > self.min_residual):
                     self._propose(gi)
             if self.cool > 0:
                 self.cool -= 1

@@ -137,7 +137,7 @@ class SCF:
 
     def __init__(self, x, y, z, w, nuclei, charges, psi0, eps0, n_electrons, gauge_shift=-0.5, mixing=0.5,
                  history=10, precision="mixed", theta=0.7, degree=7, source_leaf=2000, target_leaf=2000,
-                 soft=0.0, graph=True, extrapolator=None):
+                 soft=0.0, graph=True, extrapolator=None, orbital_mixing=5):
         t = lambda a: torch.as_tensor(np.ascontiguousarray(a), dtype=torch.float64, device="cuda")
         self.x, self.y, self.z, self.w = t(x), t(y), t(z), t(w)
         self.n = int(self.w.numel())
@@ -154,6 +154,8 @@ class SCF:
         self.stream.synchronize()
         self.use_graph = graph
         self.extrapolator = extrapolator
+        if orbital_mixing:
+            self.gi.enable_anderson(history=orbital_mixing)
         self.enuc = nuclear_repulsion(self.nuclei, self.charges)
         self.history = []
 
@@ -211,10 +213,14 @@ class SCF:
         self.gi.step()
         if self.use_graph and self.gi._graph is None:
             self.gi.capture()
+        if self.gi.anderson is not None:
+            self.stream.synchronize()
+            self.gi.anderson_step(float(self.gi.res.max().item()))
 
     def green_iterations(self, tol, max_sweeps, min_sweeps=1):
         """Sweeps until the largest orbital residual (with eigenvalue) is below tol."""
         sweeps, res = 0, float("inf")
+        self.gi.reset_anderson()  # a new potential: earlier sweeps do not mix with this one's
         if self.extrapolator is not None:
             self.extrapolator.reset()  # a new potential: earlier iterates no longer predict this one
         while sweeps < max_sweeps:
