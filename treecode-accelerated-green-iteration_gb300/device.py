@@ -77,7 +77,7 @@ class TreecodePlan:
 
     def convolve(self, target_values, source_values, kernel=Kernel.YUKAWA, kernel_params=(1.0,),
                  singularity=Singularity.SUBTRACTION, precision="mixed", out=None, stream=None,
-                 orbitals_per_item=0):
+                 orbitals_per_item=0, targets_per_thread=0):
         """target_values [norb, nt] (or [nt]), source_values [norb, ns] -> [norb, nt].
 
         kernel_params: one row per orbital (k_i for Yukawa, alpha for Coulomb
@@ -110,7 +110,7 @@ class TreecodePlan:
         _native.check(_native.lib().tagi_plan_convolve_ex(
             self._h, norb, _dev(tv, "target_values"), _dev(sv, "source_values"), _dev(out, "out"),
             int(kernel), nkp, kptr, on_dev, int(singularity), PRECISION[precision],
-            int(orbitals_per_item), _stream(stream)))
+            int(orbitals_per_item), int(targets_per_thread), _stream(stream)))
         del keep
         return out[0] if squeeze else out
 
@@ -228,7 +228,7 @@ class Systems:
     keep them alive while this object is used."""
 
     def __init__(self, plans, num_orbitals, kernel=Kernel.YUKAWA, precision="mixed",
-                 orbitals_per_item=0, stream=None):
+                 orbitals_per_item=0, targets_per_thread=0, stream=None):
         self.plans = list(plans)
         self.norb = [int(n) for n in num_orbitals]
         if len(self.plans) != len(self.norb):
@@ -240,7 +240,7 @@ class Systems:
         h = ctypes.c_void_p()
         _native.check(_native.lib().tagi_systems_create(
             ctypes.byref(h), n, hp, no, self.kernel, PRECISION[precision], int(orbitals_per_item),
-            _stream(stream)))
+            int(targets_per_thread), _stream(stream)))
         self._h = h
 
     def info(self):
