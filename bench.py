@@ -650,10 +650,12 @@ def uneven_arm(args):
 # ---------------------------------------------------------------------------
 # Ring-molecule SCF: plain Green iteration vs the learned extrapolation
 # ---------------------------------------------------------------------------
-def ring_guess(mesh, nuclei, charges, norb=21):
-    """Atom-centred start: carbon 1s, carbon 2s, hydrogen 1s, carbon 2p_z; eigenvalue guesses."""
+def ring_guess(mesh, nuclei, charges, norb=24):
+    """Atom-centred start: carbon 1s, carbon 2s, hydrogen 1s, carbon 2p_z, carbon 2p_x;
+    eigenvalue guesses.  24 orbitals for 21 doubly occupied levels: the three unoccupied
+    buffer orbitals keep one wayward orbital from corrupting the density."""
     funcs, eps = [], []
-    for kind in ("c1s", "c2s", "h1s", "c2pz"):
+    for kind in ("c1s", "c2s", "h1s", "c2pz", "c2px"):
         for R, z in zip(nuclei, charges):
             dx, dy, dz = mesh.x - R[0], mesh.y - R[1], mesh.z - R[2]
             r = np.sqrt(dx * dx + dy * dy + dz * dz)
@@ -669,6 +671,9 @@ def ring_guess(mesh, nuclei, charges, norb=21):
             elif kind == "c2pz" and z > 1:
                 funcs.append(dz * np.exp(-1.6 * r))
                 eps.append(-0.4)
+            elif kind == "c2px" and z > 1:
+                funcs.append(dx * np.exp(-1.6 * r))
+                eps.append(-0.3)
     return np.stack(funcs[:norb]), np.array(eps[:norb])
 
 
@@ -714,7 +719,8 @@ def scf_arm(args):
         "n_gpus": 1, "steps": 1, "warmup": 0, "ms_per_step": le["seconds"] * 1e3, "higher_is_better": False,
         "scaling": "weak", "vs_baseline": None, "dtype": "f32+f64",
         "data": "synthetic ring molecule (6 C at r=2.6, 6 H at r=4.7 Bohr), seeded mesh",
-        "config": {"workload": "ring_scf_21_orbitals", "points": int(mesh.n), "orbitals": 21, "electrons": 42,
+        "config": {"workload": "ring_scf_21_occupied_orbitals", "points": int(mesh.n), "orbitals": int(len(eps0)),
+                   "occupied": 21, "electrons": 42,
                    "theta": THETA, "degree": DEGREE, "leaf": [2000, 2000], "precision": "mixed",
                    "exchange": "Slater (LDA, no correlation)", "orbital_mixing": "Anderson, history 5",
                    "density_mixing": "Anderson, history 10, beta 0.5", "mesh_build_s": mesh_s,
