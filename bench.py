@@ -62,6 +62,8 @@ def parse():
     ap.add_argument("--workload", default="hartree", choices=["hartree", "orbitals", "uneven", "scf"])
     ap.add_argument("--scf-points", type=int, default=3_000_000, help="scf workload: mesh points")
     ap.add_argument("--scf-max-iter", type=int, default=60)
+    ap.add_argument("--scf-orbitals", type=int, default=24, help="scf workload: orbitals (21 occupied)")
+    ap.add_argument("--scf-mixing", type=float, default=0.3, help="scf workload: density mixing parameter")
     ap.add_argument("--scf-time-limit", type=float, default=1500.0, help="scf workload: seconds per run")
     ap.add_argument("--fp64-sample-systems", type=int, default=2,
                     help="uneven workload: systems whose plain FP64 one-call-per-orbital time is measured")
@@ -691,7 +693,7 @@ def scf_arm(args):
     t0 = time.perf_counter()
     mesh = pkg.synthetic.mesh_with_points(nuclei, charges, 7, 8, args.scf_points)
     mesh_s = time.perf_counter() - t0
-    psi0, eps0 = ring_guess(mesh, nuclei, charges)
+    psi0, eps0 = ring_guess(mesh, nuclei, charges, args.scf_orbitals)
     gauge = -0.5
     runs = {}
     for name in ("plain", "learned"):
@@ -701,7 +703,8 @@ def scf_arm(args):
         with ClockSampler(local) as clocks:
             a = time.perf_counter()
             s = scf_mod.SCF(mesh.x, mesh.y, mesh.z, mesh.w, nuclei, charges, psi0, eps0 + gauge, 42.0,
-                            gauge_shift=gauge, source_leaf=2000, target_leaf=2000, extrapolator=ex)
+                            gauge_shift=gauge, mixing=args.scf_mixing, source_leaf=2000, target_leaf=2000,
+                            extrapolator=ex)
             out = s.run(tol=1e-5, max_scf=args.scf_max_iter, time_limit=args.scf_time_limit)
             wall = time.perf_counter() - a
         runs[name] = dict(converged=out["converged"], seconds=wall, scf_iterations=out["iterations"],
@@ -723,7 +726,7 @@ def scf_arm(args):
                    "occupied": 21, "electrons": 42,
                    "theta": THETA, "degree": DEGREE, "leaf": [2000, 2000], "precision": "mixed",
                    "exchange": "Slater (LDA, no correlation)", "orbital_mixing": "Anderson, history 5",
-                   "density_mixing": "Anderson, history 10, beta 0.5", "mesh_build_s": mesh_s,
+                   "density_mixing": f"Anderson, history 10, beta {args.scf_mixing}", "mesh_build_s": mesh_s,
                    "step": "one full SCF run from the atom-centred guess"},
         "plain": pl, "learned": le, "speedup_learned_vs_plain": pl["seconds"] / le["seconds"],
         "clocks": le["clocks"], "gpu_launches": le["launches"],
