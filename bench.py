@@ -62,7 +62,7 @@ def parse():
     ap.add_argument("--workload", default="hartree", choices=["hartree", "orbitals", "uneven", "scf"])
     ap.add_argument("--scf-points", type=int, default=3_000_000, help="scf workload: mesh points")
     ap.add_argument("--scf-max-iter", type=int, default=60)
-    ap.add_argument("--scf-orbitals", type=int, default=24, help="scf workload: orbitals (21 occupied)")
+    ap.add_argument("--scf-orbitals", type=int, default=21, help="scf workload: orbitals (21 occupied)")
     ap.add_argument("--scf-mixing", type=float, default=0.3, help="scf workload: density mixing parameter")
     ap.add_argument("--scf-time-limit", type=float, default=1500.0, help="scf workload: seconds per run")
     ap.add_argument("--fp64-sample-systems", type=int, default=2,
