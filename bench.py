@@ -50,7 +50,7 @@ METRIC = "orbital convs/s at 1e-6 rel err; wall time to 1e-5 Ha SCF: chosen vs p
 UNIT = "convolutions/s"
 THETA, DEGREE = 0.7, 7
 LEAF = {"hartree": (2000, 2000), "orbitals": (2000, 2000)}
-PAIR_FLOPS = {"coulomb_ss": 14, "yukawa_ss": 15}  # FP32 pipe ops counted per pair (see DESIGN)
+PAIR_FLOPS = {"coulomb_ss": 14, "yukawa_ss": 15}  # FP32 pipe operations counted per pair in the near-tile loop
 
 
 def parse():
@@ -440,7 +440,7 @@ def gb300_arm(args):
 # Uneven multi-system batch: one persistent launch per pass, CUDA graph
 # ---------------------------------------------------------------------------
 UNEVEN_LEAVES = ((1000, 1000), (2000, 1000), (2000, 2000), (4000, 2000))
-PLAIN_LEAF = 500  # the reference's callers pass 500-point leaves (BASELINE config 1 parameters)
+PLAIN_LEAF = 500  # 500-point leaves, the tree parameters the reference's single-atom runs use
 
 
 def uneven_arm(args):
