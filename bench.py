@@ -59,7 +59,7 @@ def parse():
     ap.add_argument("--steps", type=int, default=5)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
-    ap.add_argument("--workload", default="hartree", choices=["hartree", "orbitals", "uneven", "scf"])
+    ap.add_argument("--workload", default="hartree", choices=["hartree", "orbitals", "uneven", "scf", "mesh"])
     ap.add_argument("--scf-points", type=int, default=3_000_000, help="scf workload: mesh points")
     ap.add_argument("--scf-max-iter", type=int, default=60)
     ap.add_argument("--scf-orbitals", type=int, default=21, help="scf workload: orbitals (21 occupied)")
@@ -735,10 +735,124 @@ def scf_arm(args):
     return 0
 
 
+# Two-level mesh of the ring molecule by the reference's coarsenedUniformTwoLevel
+# rule: domain [-20, 20]^3, base cells of side 5, order 7, near spacing h = 1,
+# far spacing H = 5, ball radius r = 2, level -2 (8 fine children per cell
+# within 1.5 r of a nucleus): 5,104 cells, 2.61M coarse + 14.3M fine points.
+MESH_CFG = dict(XL=20.0, max_side=5.0, order=7, h=1.0, H=5.0, r=2.0, level=-2.0)
+
+
+def mesh_arm(args):
+    """Device mesh generation (tagi_mesh_refine + tagi_mesh_points).  value =
+    mesh points (coarse + fine) generated per second with the base cells and
+    nuclei already on the device; e2e = the same through mesh.build_mesh from
+    host parameters with every mesh array read back to the host."""
+    import torch
+    ws, rank, local = dist_env()
+    torch.cuda.set_device(local)
+    pkg = importlib.import_module(PKG)
+    M = importlib.import_module(PKG + ".mesh")
+    L = pkg._native.lib()
+    c = MESH_CFG
+    nuclei, _ = pkg.synthetic.ring_molecule()
+    order = c["order"]
+    base = M.base_cells(c["XL"], c["XL"], c["XL"], c["max_side"])
+    tables = M.unit_tables(order)
+    base_d = torch.as_tensor(base, device="cuda")
+    atoms_d = torch.as_tensor(np.ascontiguousarray(nuclei, np.float64), device="cuda")
+    stream = torch.cuda.Stream()
+
+    def step():
+        cells, ppc_c, ppc_f, nfine = M.refine_cells(base_d, atoms_d, order, c["h"], c["H"], c["r"], c["level"],
+                                                    stream=stream)
+        C, F = M.mesh_points(cells, ppc_f, order, nfine, tables, stream=stream)
+        return cells, ppc_f, C, F
+
+    with torch.cuda.stream(stream):
+        for _ in range(max(args.warmup, 3)):
+            out = step()
+        ncell, nc, nf = out[0][0].numel(), out[2][0].numel(), out[3][0].numel()
+        # the points pass alone (coarse + fine kernels), CUDA events on its stream
+        ev = [torch.cuda.Event(enable_timing=True) for _ in range(2)]
+        pts_ms = []
+        for _ in range(5):
+            ev[0].record(stream)
+            M.mesh_points(out[0], out[1], order, nf, tables, stream=stream)
+            ev[1].record(stream)
+            stream.synchronize()
+            pts_ms.append(ev[0].elapsed_time(ev[1]))
+        del out
+        torch.cuda.synchronize()
+        n0 = L.tagi_launch_count()
+        with ClockSampler(local) as clocks:
+            t0 = torch.cuda.Event(enable_timing=True)
+            t1 = torch.cuda.Event(enable_timing=True)
+            t0.record(stream)
+            for _ in range(args.steps):
+                out = step()
+                del out
+            t1.record(stream)
+            stream.synchronize()
+        total_ms = t0.elapsed_time(t1)
+        launches = int(L.tagi_launch_count() - n0)
+    pts = nc + nf
+    ms = total_ms / args.steps
+    # e2e: host parameters in, every mesh array back on the host
+    e2e_ms = []
+    d2h = 0
+    for _ in range(args.steps):
+        a = time.perf_counter()
+        m = M.build_mesh(c["XL"], c["max_side"], nuclei, order, c["h"], c["H"], c["r"], c["level"],
+                         tables=tables)
+        host = [t.cpu() for t in (m.X, m.Y, m.Z, m.W, m.Xf, m.Yf, m.Zf, m.Wf, m.cellX, m.cellY, m.cellZ,
+                                  m.cellDX, m.cellDY, m.cellDZ, m.PtsPerCellCoarse, m.PtsPerCellFine)]
+        torch.cuda.synchronize()
+        e2e_ms.append((time.perf_counter() - a) * 1e3)
+        d2h = sum(h.numel() * h.element_size() for h in host)
+        del m, host
+    pts_med = statistics.median(pts_ms)
+    alg_bytes = 32 * pts + 56 * ncell
+    peaks = {}
+    try:
+        with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as f:
+            peaks = json.load(f)
+    except OSError:
+        pass
+    peak = peaks.get("hbm_gbs") or 6800.0
+    achieved = alg_bytes / (pts_med * 1e-3) / 1e9
+    line = {"metric": "mesh points/s (two-level first-kind mesh, refinement + points)",
+            "value": pts / (ms * 1e-3), "unit": "points/s", "n_gpus": 1, "steps": args.steps,
+            "warmup": max(args.warmup, 3), "ms_per_step": ms, "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "f64", "data": "synthetic ring molecule (12 nuclei), seeded",
+            "config": {"workload": "ring_two_level_mesh", **c, "cells": int(ncell), "coarse_points": int(nc),
+                       "fine_points": int(nf), "l2": "outputs (541 MB) larger than L2"},
+            "roofline": {"bound": "hbm", "kernel": "points pass (mesh_coarse_points + mesh_fine_points)",
+                         "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
+                         "traffic": None, "bytes_per_launch": alg_bytes, "ms": pts_med,
+                         "peak_source": "measured" if "hbm_gbs" in peaks else "fallback"},
+            "e2e": {"value": pts / (statistics.median(e2e_ms) * 1e-3), "unit": "points/s",
+                    "h2d_bytes_per_step": int(base.nbytes + nuclei.nbytes), "d2h_bytes_per_step": int(d2h)},
+            "clocks": clocks.summary(), "gpu_launches": launches}
+    if not args.no_cpu_baseline:
+        from oracle import mesh_oracle as MO
+        a = time.perf_counter()
+        lv = MO.refine(base, nuclei, c["h"], c["H"], c["r"], c["level"])
+        tab = MO.cell_table(lv, order)
+        MO.points(tab, order, *tables)
+        secs = time.perf_counter() - a
+        line["cpu_baseline"] = {"value": pts / secs, "unit": "points/s", "cores": 1, "kind": "port",
+                                "sample": "the whole mesh by the oracle's restatement (Python recursion, "
+                                          "numpy per cell)"}
+    print(json.dumps(line), flush=True)
+    return 0
+
+
 def main():
     args = parse()
     if args.impl == "reference":
         return reference_arm(args)
+    if args.workload == "mesh":
+        return mesh_arm(args)
     if args.workload == "uneven":
         return uneven_arm(args)
     if args.workload == "scf":

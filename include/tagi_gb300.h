@@ -360,6 +360,49 @@ int tagi_interp_dev(const double *coarseX, const double *coarseY, const double *
                     double *fineF, const int *pointsPerCell_fine, int fineN, int numberOfCells,
                     int cellOrder, void *stream);
 
+/* Mesh generation on the device, in two calls.
+ *
+ * tagi_mesh_refine replaces the per-cell refinement the reference runs in
+ * Python for the "coarsenedUniformTwoLevel" divide criterion
+ * (mpiMeshBuilding.py:402-421 refineCellReturnCells -> TreeStruct_CC.py:1049
+ * recursiveDivide -> CellStruct_CC.py:2344 refineCoarseningUniform_TwoLevel,
+ * then TreeStruct_CC.py:2360 extractCellXYZ).  baseCells: device
+ * [numBase x 6] rows (xmin, xmax, ymin, ymax, zmin, zmax), the rows
+ * inializeBaseMesh_distributed returns (mpiMeshBuilding.py:103); atomXYZ:
+ * device [numAtoms x 3].  h, H, r, level are divideParameter1..4 (near
+ * spacing, far spacing, ball radius, level); cells below minDepth always
+ * divide (the tree's minDepth); a cell at maxDepth (<= 16) that the rule would
+ * divide is an error.  Writes the leaf cells depth first, children x-major
+ * (the reference's uniqueID order), as centre (cellX..Z), width
+ * (cellDX..DZ), (order+1)^3 points per coarse cell and 1, 8, 27 or 64 times
+ * that per fine cell: the arrays extractCellXYZ returns.  cellX == NULL
+ * counts only.  numCells / numCoarsePoints / numFinePoints (host) receive the
+ * counts, also when capacity is too small (TAGI_ERR_ARG).  Synchronizes the
+ * stream once per refinement level.
+ *
+ * tagi_mesh_points replaces the point loop of buildMeshFromMinimumDepthCells
+ * (mpiMeshBuilding.py:517-556: coarseQuadraturePointsSingleCell and
+ * fineQuadraturePointsSingleCell): the coarse mesh X, Y, Z, W
+ * [numCoarsePoints] and, when Xf..Wf are given, the two-level fine mesh
+ * [numFinePoints] of the cell table.  unitNodes / unitWeights (host,
+ * order+1 each) are the first-kind nodes cos(theta_i) on [-1, 1] and the
+ * unscaled weights (meshUtilities.py:835-883); NULL for both computes them
+ * with libm.  Results are bit-identical to the reference's for the same
+ * tables.  These two entry points have no device counterpart in the
+ * reference. */
+int tagi_mesh_refine(const double *baseCells, int numBase, const double *atomXYZ, int numAtoms,
+                     int order, double h, double H, double r, double level, int minDepth,
+                     int maxDepth, double *cellX, double *cellY, double *cellZ, double *cellDX,
+                     double *cellDY, double *cellDZ, int *ptsPerCellCoarse, int *ptsPerCellFine,
+                     int capacity, int *numCells, long long *numCoarsePoints,
+                     long long *numFinePoints, void *stream);
+int tagi_mesh_points(const double *cellX, const double *cellY, const double *cellZ,
+                     const double *cellDX, const double *cellDY, const double *cellDZ,
+                     const int *ptsPerCellFine, int numCells, int order, const double *unitNodes,
+                     const double *unitWeights, double *X, double *Y, double *Z, double *W,
+                     long long numCoarsePoints, double *Xf, double *Yf, double *Zf, double *Wf,
+                     long long numFinePoints, void *stream);
+
 /* ---------------------------------------------------------------------- */
 /* 3. Configuration and errors.                                            */
 /* ---------------------------------------------------------------------- */

@@ -5,7 +5,9 @@ Run here, where the reference tree is mounted (it is not on the GPU machine):
 It needs oracle/_ref (``make -C oracle ref``: the reference's own
 Orthogonalization.c and TwoMeshInterpolation.c compiled from their sources)
 and imports the reference's Python meshUtilities.py for the Chebyshev
-first-kind points and weights.  Outputs (small .npz files) are committed.
+first-kind points and weights, and mpiMeshBuilding.py / CellStruct_CC.py for
+the two-level mesh (refinement rule and cell points).  Outputs (small .npz
+files) are committed.
 """
 import os
 import sys
@@ -136,6 +138,131 @@ def mesh_golden(mu):
     np.savez_compressed(os.path.join(HERE, "mesh_reference.npz"), **out)
 
 
+REF_DATA = "/root/reference/3D-GreenIteration/src/dataStructures"
+
+
+def reference_mesh_building():
+    """Import the reference's mpiMeshBuilding.py and CellStruct_CC.py on one
+    rank: mpi4py is a one-rank stand-in; the tree, atom, Zoltan, memory
+    tracker and grid-point modules, which the imported functions do not use
+    here, are empty stand-ins."""
+    class _Comm:
+        def Get_rank(self):
+            return 0
+
+        def Get_size(self):
+            return 1
+
+        def barrier(self):
+            pass
+
+        def allreduce(self, v):
+            return v
+
+    mpi = types.ModuleType("mpi4py")
+    mpi.MPI = types.SimpleNamespace(COMM_WORLD=_Comm(), Wtime=lambda: 0.0)
+    sys.modules["mpi4py"] = mpi
+    sys.modules["mpi4py.MPI"] = mpi.MPI
+    for name in ("pympler", "TreeStruct_CC", "AtomStruct", "zoltan_wrapper", "GridpointStruct"):
+        m = types.ModuleType(name)
+        m.tracker = m.classtracker = m.Tree = m.Atom = m.callZoltan = None
+        m.GridPoint = lambda *a, **k: None
+        sys.modules[name] = m
+    sys.modules.setdefault("vtk", types.ModuleType("vtk"))
+    sys.modules.setdefault("interpolation_wrapper", types.ModuleType("interpolation_wrapper"))
+    import scipy.special
+    if not hasattr(scipy.special, "sph_harm"):
+        scipy.special.sph_harm = None
+    sys.path[:0] = [REF_UTIL, REF_DATA]
+    import CellStruct_CC
+    import mpiMeshBuilding
+    return mpiMeshBuilding, CellStruct_CC
+
+
+def mesh_build_golden():
+    """A whole two-level mesh made by the reference's own functions:
+    base cells by inializeBaseMesh_distributed (mpiMeshBuilding.py:68-124),
+    each cell's decision by Cell.refineCoarseningUniform_TwoLevel
+    (CellStruct_CC.py:2344-2491) on a stand-in cell object, and the points by
+    coarse/fineQuadraturePointsSingleCell (mpiMeshBuilding.py:725-840).  The
+    recursion driving the rule restates recursiveDivide
+    (TreeStruct_CC.py:1049-1140): midpoint split, children x-major, depth
+    first, which is the uniqueID order extractCellXYZ walks."""
+    mb, cs = reference_mesh_building()
+    out = {}
+    cases = {
+        # domain, base side, atoms, order, h, H, r, level
+        "a": (8.0, 4.0, [[0.3, -0.2, 0.1], [-2.6, 1.45, 2.05]], 3, 1.0, 4.0, 1.0, -2.0),
+        "b": (6.0, 3.0, [[0.05, 0.4, -1.3]], 2, 0.75, 3.0, 1.5, -3.0),
+        "c": (5.0, 2.5, [[1.1, -0.7, 0.2], [-1.9, 0.3, -2.2], [0.0, 2.4, 1.0]], 2, 0.6, 2.5, 0.8, 1.0),
+    }
+    for tag, (XL, side, atoms, order, h, H, r, level) in cases.items():
+        _, _, _, cells = mb.inializeBaseMesh_distributed(XL, XL, XL, side, verbose=0)
+        atom_objs = [types.SimpleNamespace(x=a[0], y=a[1], z=a[2]) for a in atoms]
+        tree = types.SimpleNamespace(atoms=atom_objs)
+        uw = mb.unscaledWeightsFirstKind(order)
+        leaves = []
+
+        def visit(b, depth):
+            c = types.SimpleNamespace(xmin=b[0], xmax=b[1], ymin=b[2], ymax=b[3], zmin=b[4], zmax=b[5],
+                                      px=order, py=order, pz=order, tree=tree, unscaledW=uw,
+                                      numCoarsePoints=(order + 1) ** 3)
+            c.w = mb.weights3DFirstKind(b[0], b[1], order, b[2], b[3], order, b[4], b[5], order, uw)
+            cs.Cell.refineCoarseningUniform_TwoLevel(c, h, H, r, level)
+            if not c.divideFlag:
+                leaves.append((b, int(c.numFinePoints) if c.fineMesh else int(c.numCoarsePoints)))
+                return
+            xd, yd, zd = (b[1] + b[0]) / 2, (b[3] + b[2]) / 2, (b[5] + b[4]) / 2
+            xb = np.array([b[0], float(xd), b[1]])
+            yb = np.array([b[2], float(yd), b[3]])
+            zb = np.array([b[4], float(zd), b[5]])
+            for i in range(2):
+                for j in range(2):
+                    for k in range(2):
+                        visit((xb[i], xb[i + 1], yb[j], yb[j + 1], zb[k], zb[k + 1]), depth + 1)
+
+        for row in cells:
+            visit(tuple(row), 0)
+        cx = np.array([(b[0] + b[1]) / 2 for b, _ in leaves])
+        cy = np.array([(b[2] + b[3]) / 2 for b, _ in leaves])
+        cz = np.array([(b[4] + b[5]) / 2 for b, _ in leaves])
+        dx = np.array([b[1] - b[0] for b, _ in leaves])
+        dy = np.array([b[3] - b[2] for b, _ in leaves])
+        dz = np.array([b[5] - b[4] for b, _ in leaves])
+        ppc_f = np.array([n for _, n in leaves], np.int32)
+        C, F = [[], [], [], []], [[], [], [], []]
+        for c in range(len(leaves)):
+            xl, xh = cx[c] - dx[c] / 2, cx[c] + dx[c] / 2
+            yl, yh = cy[c] - dy[c] / 2, cy[c] + dy[c] / 2
+            zl, zh = cz[c] - dz[c] / 2, cz[c] + dz[c] / 2
+            pc = mb.coarseQuadraturePointsSingleCell(xl, xh, yl, yh, zl, zh, order)
+            if ppc_f[c] == (order + 1) ** 3:
+                pf = tuple(np.copy(a) for a in pc)
+            else:
+                pf = mb.fineQuadraturePointsSingleCell(xl, xh, yl, yh, zl, zh, order, int(ppc_f[c]))
+            for a, v in zip(C, pc):
+                a.append(v)
+            for a, v in zip(F, pf):
+                a.append(v)
+        C = [np.concatenate(a) for a in C]
+        F = [np.concatenate(a) for a in F]
+        ends = np.linspace(np.pi, 0, order + 2)
+        out.update({f"{tag}_params": np.array([XL, side, order, h, H, r, level]),
+                    f"{tag}_atoms": np.array(atoms, np.float64), f"{tag}_base": np.asarray(cells, np.float64),
+                    f"{tag}_u": np.cos((ends[1:] + ends[:-1]) / 2), f"{tag}_W": uw,
+                    f"{tag}_cx": cx, f"{tag}_cy": cy, f"{tag}_cz": cz, f"{tag}_dx": dx, f"{tag}_dy": dy,
+                    f"{tag}_dz": dz, f"{tag}_ppc_f": ppc_f})
+        # The meshes themselves as SHA-256 digests of their float64 bytes,
+        # plus every 97th point, to keep the file small.
+        for name, arr in zip(("x", "y", "z", "w", "xf", "yf", "zf", "wf"), C + F):
+            out[f"{tag}_{name}_sha256"] = np.frombuffer(
+                __import__("hashlib").sha256(np.ascontiguousarray(arr, np.float64).tobytes()).digest(),
+                np.uint8)
+            out[f"{tag}_{name}_every97"] = arr[::97]
+            out[f"{tag}_{name}_len"] = np.array(len(arr))
+    np.savez_compressed(os.path.join(HERE, "mesh_build_reference.npz"), **out)
+
+
 if __name__ == "__main__":
     O.build(ref=True)
     if not O.ref_available():
@@ -144,4 +271,5 @@ if __name__ == "__main__":
     mgs_golden()
     interp_golden(mu)
     mesh_golden(mu)
+    mesh_build_golden()
     print("golden vectors written to", HERE)

@@ -1,0 +1,99 @@
+"""Mesh generation on the host side (no GPU): the oracle's restatement of the
+reference's two-level mesh is pinned against the reference itself
+(tests/golden/mesh_build_reference.npz, made by make_golden.py from the
+reference's own divide rule and cell-point functions), bit for bit; the
+package's host helpers (base cells, 1-D tables) equal the oracle's."""
+import hashlib
+import importlib
+import os
+
+import numpy as np
+import pytest
+
+from oracle import mesh_oracle as MO
+
+GOLD = os.path.join(os.path.dirname(__file__), "golden", "mesh_build_reference.npz")
+CASES = ("a", "b", "c")
+
+
+def digest(a):
+    return np.frombuffer(hashlib.sha256(np.ascontiguousarray(a, np.float64).tobytes()).digest(), np.uint8)
+
+
+@pytest.fixture(scope="module")
+def gold():
+    return np.load(GOLD)
+
+
+@pytest.fixture(scope="module")
+def M(pkg):
+    return importlib.import_module(pkg.__name__ + ".mesh")
+
+
+def case(g, t):
+    XL, side, order, h, H, r, level = g[f"{t}_params"]
+    return float(XL), float(side), int(order), float(h), float(H), float(r), float(level)
+
+
+@pytest.mark.parametrize("t", CASES)
+def test_oracle_cells_match_reference(gold, t):
+    XL, side, order, h, H, r, level = case(gold, t)
+    base = MO.base_cells(XL, XL, XL, side)
+    assert np.array_equal(base, gold[f"{t}_base"])
+    leaves = MO.refine(base, gold[f"{t}_atoms"], h, H, r, level)
+    tab = MO.cell_table(leaves, order)
+    for k in ("cx", "cy", "cz", "dx", "dy", "dz", "ppc_f"):
+        assert np.array_equal(tab[k], gold[f"{t}_{k}"]), k
+
+
+@pytest.mark.parametrize("t", CASES)
+def test_oracle_points_match_reference(gold, t):
+    XL, side, order, h, H, r, level = case(gold, t)
+    tab = {k: gold[f"{t}_{k}"] for k in ("cx", "cy", "cz", "dx", "dy", "dz", "ppc_f")}
+    pts = MO.points(tab, order, gold[f"{t}_u"], gold[f"{t}_W"])
+    for name, a in zip(("x", "y", "z", "w", "xf", "yf", "zf", "wf"), pts):
+        assert len(a) == int(gold[f"{t}_{name}_len"]), name
+        assert np.array_equal(a[::97], gold[f"{t}_{name}_every97"]), name
+        assert np.array_equal(digest(a), gold[f"{t}_{name}_sha256"]), name
+
+
+def test_fixture_covers_the_rule(gold):
+    """The fixture holds unrefined and fine cells of 8 and 27 children and a
+    level >= 1 case (the r/2 branch)."""
+    ppc = {t: set(np.unique(gold[f"{t}_ppc_f"] // (case(gold, t)[2] + 1) ** 3)) for t in CASES}
+    assert ppc["a"] == {1, 8} and ppc["b"] == {1, 27} and ppc["c"] == {1}
+    assert case(gold, "c")[6] >= 1
+
+
+@pytest.mark.parametrize("t", CASES)
+def test_weights_sum_to_volume(gold, t):
+    """mpiMeshBuilding.py:456-459 checks the cell volumes; the quadrature weights
+    integrate 1 exactly, so both meshes' weights sum to the domain volume."""
+    XL, side, order, h, H, r, level = case(gold, t)
+    tab = {k: gold[f"{t}_{k}"] for k in ("cx", "cy", "cz", "dx", "dy", "dz", "ppc_f")}
+    x, y, z, w, xf, yf, zf, wf = MO.points(tab, order)
+    vol = (2 * XL) ** 3
+    assert abs(w.sum() - vol) / vol < 1e-12 and abs(wf.sum() - vol) / vol < 1e-12
+    assert abs(np.sum(tab["dx"] * tab["dy"] * tab["dz"]) - vol) / vol < 1e-14
+
+
+@pytest.mark.parametrize("t", CASES)
+def test_package_host_helpers_match_oracle(M, gold, t):
+    XL, side, order, *_ = case(gold, t)
+    assert np.array_equal(M.base_cells(XL, XL, XL, side), MO.base_cells(XL, XL, XL, side))
+    u, W = M.unit_tables(order)
+    assert np.array_equal(u, MO.unit_nodes(order)) and np.array_equal(W, MO.unit_weights(order))
+    # here (where the fixture was made) they are the reference's tables too
+    assert np.array_equal(u, gold[f"{t}_u"]) and np.array_equal(W, gold[f"{t}_W"])
+
+
+def test_base_cells_uneven_domain(M):
+    """Non-cubic domain and a side that does not divide it (ceil rule, linspace)."""
+    b = M.base_cells(7.0, 5.0, 3.0, 2.5)
+    assert b.shape == (6 * 4 * 3, 6)
+    assert np.array_equal(b, MO.base_cells(7.0, 5.0, 3.0, 2.5))
+
+
+def test_oracle_rejects_depth_overflow():
+    with pytest.raises(ValueError):
+        MO.refine(MO.base_cells(4.0, 4.0, 4.0, 8.0), [[0.1, 0.2, 0.3]], 0.01, 8.0, 1.0, -2.0, max_depth=3)

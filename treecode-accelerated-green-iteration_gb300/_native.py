@@ -85,6 +85,10 @@ SIGNATURES = {
     "tagi_mgs_dev": (_i, [_vp, _vp, _vp, _i, _i, _i, _vp]),
     "tagi_mgs_dev_noalloc": (_i, [_vp, _vp, _vp, _i, _i, _i, _vp]),
     "tagi_interp_dev": (_i, [_vp, _vp, _vp, _vp, _vp, _i, _vp, _vp, _vp, _vp, _vp, _i, _i, _i, _vp]),
+    "tagi_mesh_refine": (_i, [_vp, _i, _vp, _i, _i, _d, _d, _d, _d, _i, _i] + [_vp] * 8 +
+                         [_i, _ip, ctypes.POINTER(ctypes.c_longlong), ctypes.POINTER(ctypes.c_longlong), _vp]),
+    "tagi_mesh_points": (_i, [_vp] * 7 + [_i, _i, _dp, _dp] + [_vp] * 4 + [ctypes.c_longlong] + [_vp] * 4 +
+                         [ctypes.c_longlong, _vp]),
     "tagi_set_precision": (_i, [_i]),
     "tagi_get_precision": (_i, []),
     "tagi_beta_parameters": (_i, [_d, _dp, _ip, _ip, _ip]),
