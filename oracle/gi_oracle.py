@@ -12,6 +12,10 @@ with every orbital advanced in the same sweep, as the device sweep does:
   (scfFixedPoint.py:62-67).
 The convolution is the oracle's FP64 treecode (same tree and list rules as
 the device), so an FP64 device sweep matches this one to rounding.
+
+two_mesh_correction restates the eigenvalue correction of
+Green-Iteration-Routines/twoMeshCorrection.py:172-441 (all-electron, local
+potentials) with the oracle's interpolation and treecode.
 """
 import math
 
@@ -78,3 +82,39 @@ def anderson(rin_hist, rout_hist, w, beta):
         win += c[k] * (rin_hist[n - 2 - k] - rin_hist[-1])
         wout += c[k] * (rout_hist[n - 2 - k] - rout_hist[-1])
     return beta * wout + (1 - beta) * win
+
+
+def two_mesh_correction(coarse, fine, ppc_c, ppc_f, order, nuclei, charges, psi, eps, rho, theta, degree,
+                        source_leaf, target_leaf, gauge=-0.5, alpha=1.0):
+    """Eigenvalue corrections of twoMeshCorrection.py:172-441 (all-electron,
+    local potentials, Slater exchange): the oracle's interpolation and FP64
+    treecode (coarse targets, fine sources, theta - 0.15, degree + 2).
+    coarse = (X, Y, Z, W), fine = (Xf, Yf, Zf, Wf).  Returns (dE, V_H, E_H)."""
+    X, Y, Z, W = (np.asarray(a, np.float64) for a in coarse)
+    Xf, Yf, Zf, Wf = (np.asarray(a, np.float64) for a in fine)
+    ncells = len(ppc_c)
+
+    def interp(F):
+        return O.interp(X, Y, Z, F, ppc_c, Xf, Yf, Zf, ppc_f, ncells, order)
+
+    def vext(x, y, z):
+        v = np.zeros_like(x)
+        for R, Zc in zip(np.asarray(nuclei, np.float64).reshape(-1, 3), np.asarray(charges, np.float64)):
+            v -= Zc / np.sqrt((x - R[0]) ** 2 + (y - R[1]) ** 2 + (z - R[2]) ** 2)
+        return v
+
+    plan = O.Plan(X, Y, Z, Xf, Yf, Zf, Wf, theta - 0.15, degree + 2, source_leaf, target_leaf)
+    COULOMB = 1
+    vh = plan.convolve(rho, interp(rho), Wf, COULOMB, [alpha], SUBTRACTION)
+    eh = 0.5 * float(np.sum(W * rho * vh))
+    vx, _ = lda_exchange(rho)
+    ve, ve_f = vext(X, Y, Z), vext(Xf, Yf, Zf)
+    veff = vh + vx + ve + gauge
+    veff_f = interp(veff - ve) + ve_f
+    dE = np.zeros(len(eps))
+    for m in range(len(eps)):
+        pf = interp(psi[m])
+        c = plan.convolve(-2.0 * psi[m] * veff, -2.0 * pf * veff_f, Wf, YUKAWA, [math.sqrt(-2.0 * eps[m])],
+                          SUBTRACTION) / (4.0 * math.pi)
+        dE[m] = -np.sum(W * psi[m] * veff * (psi[m] - c)) / np.sum(W * c * c)
+    return dE, vh, eh

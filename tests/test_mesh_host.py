@@ -97,3 +97,26 @@ def test_base_cells_uneven_domain(M):
 def test_oracle_rejects_depth_overflow():
     with pytest.raises(ValueError):
         MO.refine(MO.base_cells(4.0, 4.0, 4.0, 8.0), [[0.1, 0.2, 0.3]], 0.01, 8.0, 1.0, -2.0, max_depth=3)
+
+
+def test_two_mesh_oracle_identity_mesh(oracle):
+    """The oracle's two-mesh correction with fine mesh == coarse mesh (no fine
+    cells) is one Harrison update at theta - 0.15, degree + 2."""
+    import math
+    from oracle import gi_oracle as G
+    nuc, chg = np.array([[0.3, -0.2, 0.1]]), np.array([1.0])
+    tab, (X, Y, Z, W, Xf, Yf, Zf, Wf) = MO.build(4.0, 4.0, nuc, 2, 1.0, 4.0, 1.0, 0.0)
+    assert np.array_equal(X, Xf) and np.array_equal(W, Wf)
+    r = np.sqrt((X - 0.3) ** 2 + (Y + 0.2) ** 2 + (Z - 0.1) ** 2)
+    psi = np.exp(-r)[None, :]
+    psi /= np.sqrt((psi ** 2 * W).sum())
+    rho = 2 * psi[0] ** 2
+    dE, vh, eh = G.two_mesh_correction((X, Y, Z, W), (Xf, Yf, Zf, Wf), tab["ppc_c"], tab["ppc_f"], 2, nuc, chg,
+                                       psi, np.array([-0.5]), rho, 0.7, 5, 200, 200)
+    plan = oracle.Plan(X, Y, Z, X, Y, Z, W, 0.55, 7, 200, 200)
+    vh1 = plan.convolve(rho, rho, W, 1, [1.0], 2)
+    assert np.array_equal(vh, vh1)
+    veff = vh1 + G.lda_exchange(rho)[0] - 1.0 / r - 0.5
+    c = plan.convolve(-2 * psi[0] * veff, -2 * psi[0] * veff, W, 2, [1.0], 2) / (4 * math.pi)
+    d = -np.sum(W * psi[0] * veff * (psi[0] - c)) / np.sum(W * c * c)
+    assert abs(dE[0] - d) <= 1e-12 * max(1.0, abs(d))

@@ -194,6 +194,9 @@ __global__ void __launch_bounds__(MT) mesh_cell_table(const int *__restrict__ or
     if (ppc_f) ppc_f[i] = leaf_fine[s] * p3;
 }
 
+// x/2 and x/4 are written as products with 0.5 and 0.25: the same correctly
+// rounded value as the reference's divisions, without a division sequence.
+
 // One cell's bounds from centre and width: xl = cx - dx/2, xh = cx + dx/2
 // (mpiMeshBuilding.py:519-527).
 __device__ __forceinline__ void cell_bounds(const double *cx, const double *cy, const double *cz,
@@ -203,48 +206,9 @@ __device__ __forceinline__ void cell_bounds(const double *cx, const double *cy, 
     const double wid[3] = {dx[c], dy[c], dz[c]};
 #pragma unroll
     for (int d = 0; d < 3; d++) {
-        const double hw = __ddiv_rn(wid[d], 2.0);
+        const double hw = __dmul_rn(wid[d], 0.5);
         lo[d] = __dsub_rn(ctr[d], hw);
         hi[d] = __dadd_rn(ctr[d], hw);
-    }
-}
-
-// One point of a cell [lo, hi]^3 at node (i, j, k): x = lo + (hi-lo)/2 (u+1),
-// w = ((hx W_i)(hy W_j))(hz W_k)  (meshUtilities.py:857-883).
-__device__ __forceinline__ void cell_point(const Tables &t, const double lo[3], const double hi[3], int i,
-                                           int j, int k, double *X, double *Y, double *Z, double *W,
-                                           long o) {
-    const int idx[3] = {i, j, k};
-    double pt[3], wt[3];
-#pragma unroll
-    for (int d = 0; d < 3; d++) {
-        const double hw = __ddiv_rn(__dsub_rn(hi[d], lo[d]), 2.0);
-        pt[d] = __dadd_rn(lo[d], __dmul_rn(hw, __dadd_rn(t.u[idx[d]], 1.0)));
-        wt[d] = __dmul_rn(hw, t.w[idx[d]]);
-    }
-    X[o] = pt[0];
-    Y[o] = pt[1];
-    Z[o] = pt[2];
-    W[o] = __dmul_rn(__dmul_rn(wt[0], wt[1]), wt[2]);
-}
-
-__global__ void __launch_bounds__(MT) mesh_coarse_points(const double *__restrict__ cx,
-                                                         const double *__restrict__ cy,
-                                                         const double *__restrict__ cz,
-                                                         const double *__restrict__ dx,
-                                                         const double *__restrict__ dy,
-                                                         const double *__restrict__ dz, long npts, int p1,
-                                                         const __grid_constant__ Tables t,
-                                                         double *__restrict__ X, double *__restrict__ Y,
-                                                         double *__restrict__ Z, double *__restrict__ W) {
-    const long p3 = (long)p1 * p1 * p1;
-    for (long o = (long)blockIdx.x * blockDim.x + threadIdx.x; o < npts; o += (long)gridDim.x * blockDim.x) {
-        const long c = o / p3;
-        const int loc = (int)(o - c * p3);
-        const int i = loc / (p1 * p1), j = (loc / p1) % p1, k = loc % p1;
-        double lo[3], hi[3];
-        cell_bounds(cx, cy, cz, dx, dy, dz, c, lo, hi);
-        cell_point(t, lo, hi, i, j, k, X, Y, Z, W, o);
     }
 }
 
@@ -253,18 +217,19 @@ __global__ void __launch_bounds__(MT) mesh_coarse_points(const double *__restric
 __device__ __forceinline__ double split_point(double lo, double hi, int m, int s) {
     if (s == 0) return lo;
     if (s == m) return hi;
-    if (m == 2) return __ddiv_rn(__dadd_rn(lo, hi), 2.0);
+    if (m == 2) return __dmul_rn(__dadd_rn(lo, hi), 0.5);
     if (m == 3)
         return s == 1 ? __ddiv_rn(__dadd_rn(__dmul_rn(2.0, lo), hi), 3.0)
                       : __ddiv_rn(__dadd_rn(__dmul_rn(2.0, hi), lo), 3.0);
     // m == 4
-    if (s == 2) return __ddiv_rn(__dadd_rn(lo, hi), 2.0);
-    return s == 1 ? __ddiv_rn(__dadd_rn(__dmul_rn(3.0, lo), hi), 4.0)
-                  : __ddiv_rn(__dadd_rn(__dmul_rn(3.0, hi), lo), 4.0);
+    if (s == 2) return __dmul_rn(__dadd_rn(lo, hi), 0.5);
+    return s == 1 ? __dmul_rn(__dadd_rn(__dmul_rn(3.0, lo), hi), 0.25)
+                  : __dmul_rn(__dadd_rn(__dmul_rn(3.0, hi), lo), 0.25);
 }
 
+// m (children per side) and m^3 per cell from the fine point counts.
 __global__ void mesh_fine_counts(const int *__restrict__ ppc_f, int n, int p3, int *__restrict__ sub,
-                                 int *__restrict__ err) {
+                                 int *__restrict__ nsub, int *__restrict__ err) {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= n) return;
     const int v = ppc_f[i];
@@ -275,41 +240,70 @@ __global__ void mesh_fine_counts(const int *__restrict__ ppc_f, int n, int p3, i
     else if (v == 64 * p3) m = 4;
     if (!m) atomicOr(err, 2);
     sub[i] = m;
+    nsub[i] = m * m * m;
 }
 
-__global__ void __launch_bounds__(MT) mesh_fine_points(const double *__restrict__ cx,
-                                                       const double *__restrict__ cy,
-                                                       const double *__restrict__ cz,
-                                                       const double *__restrict__ dx,
-                                                       const double *__restrict__ dy,
-                                                       const double *__restrict__ dz,
-                                                       const int *__restrict__ off, const int *__restrict__ sub,
-                                                       int ncells, long npts, int p1,
-                                                       const __grid_constant__ Tables t,
-                                                       double *__restrict__ X, double *__restrict__ Y,
-                                                       double *__restrict__ Z, double *__restrict__ W) {
-    const int p3 = p1 * p1 * p1;
-    for (long o = (long)blockIdx.x * blockDim.x + threadIdx.x; o < npts; o += (long)gridDim.x * blockDim.x) {
-        // last cell whose offset is <= o (offsets are non-decreasing, off[0] = 0)
-        int a = 0, b = ncells - 1;
-        while (a < b) {
-            const int mid = (a + b + 1) >> 1;
-            if ((long)off[mid] <= o) a = mid;
-            else b = mid - 1;
+constexpr int PW = 8;  // warps per CTA in mesh_points_warp
+
+// One warp per sub-cell: a coarse cell (sub_off == nullptr), or child
+// (ii, jj, kk) of a fine cell.  Every sub-cell holds (order+1)^3 points, so
+// sub-cell s writes points [s p3, (s+1) p3).  Lanes < order+1 evaluate the
+// 1-D nodes x = lo + (hi-lo)/2 (u+1) and scaled weights (hi-lo)/2 W of each
+// axis once (meshUtilities.py:857-883); every point is then three shared
+// loads, w = ((wx_i wy_j) wz_k) and four coalesced stores.
+__global__ void __launch_bounds__(PW * 32) mesh_points_warp(const double *__restrict__ cx,
+                                                            const double *__restrict__ cy,
+                                                            const double *__restrict__ cz,
+                                                            const double *__restrict__ dx,
+                                                            const double *__restrict__ dy,
+                                                            const double *__restrict__ dz,
+                                                            const int *__restrict__ sub_off,
+                                                            const int *__restrict__ sub, int ncells,
+                                                            long nsubcells, int p1,
+                                                            const __grid_constant__ Tables t,
+                                                            double *__restrict__ X, double *__restrict__ Y,
+                                                            double *__restrict__ Z, double *__restrict__ W) {
+    __shared__ double sh[PW][6][MESH_MAX_P1];
+    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+    const int p2 = p1 * p1, p3 = p2 * p1;
+    double(*nd)[MESH_MAX_P1] = sh[wid];
+    for (long s = (long)blockIdx.x * PW + wid; s < nsubcells; s += (long)gridDim.x * PW) {
+        int c = (int)s, m = 1, child = 0;
+        if (sub_off) {
+            // last cell whose first sub-cell is <= s (every cell has >= 1)
+            int a = 0, b = ncells - 1;
+            while (a < b) {
+                const int mid = (a + b + 1) >> 1;
+                if ((long)sub_off[mid] <= s) a = mid;
+                else b = mid - 1;
+            }
+            c = a;
+            m = sub[c];
+            child = (int)(s - sub_off[c]);
         }
-        const int c = a;
-        const int m = sub[c];
-        const int local = (int)(o - off[c]);
-        const int child = local / p3, loc = local - child * p3;
-        const int ii = child / (m * m), jj = (child / m) % m, kk = child % m;
-        double lo[3], hi[3];
-        cell_bounds(cx, cy, cz, dx, dy, dz, c, lo, hi);
-        const double clo[3] = {split_point(lo[0], hi[0], m, ii), split_point(lo[1], hi[1], m, jj),
-                               split_point(lo[2], hi[2], m, kk)};
-        const double chi[3] = {split_point(lo[0], hi[0], m, ii + 1), split_point(lo[1], hi[1], m, jj + 1),
-                               split_point(lo[2], hi[2], m, kk + 1)};
-        const int i = loc / (p1 * p1), j = (loc / p1) % p1, k = loc % p1;
-        cell_point(t, clo, chi, i, j, k, X, Y, Z, W, o);
+        if (lane < p1) {
+            double lo[3], hi[3];
+            cell_bounds(cx, cy, cz, dx, dy, dz, c, lo, hi);
+            const int ch[3] = {child / (m * m), (child / m) % m, child % m};
+#pragma unroll
+            for (int d = 0; d < 3; d++) {
+                const double l = split_point(lo[d], hi[d], m, ch[d]);
+                const double h = split_point(lo[d], hi[d], m, ch[d] + 1);
+                const double hw = __dmul_rn(__dsub_rn(h, l), 0.5);
+                nd[d][lane] = __dadd_rn(l, __dmul_rn(hw, __dadd_rn(t.u[lane], 1.0)));
+                nd[3 + d][lane] = __dmul_rn(hw, t.w[lane]);
+            }
+        }
+        __syncwarp();
+        const long base = s * p3;
+        for (int q = lane; q < p3; q += 32) {
+            const int i = q / p2, j = (q / p1) % p1, k = q % p1;
+            X[base + q] = nd[0][i];
+            Y[base + q] = nd[1][j];
+            Z[base + q] = nd[2][k];
+            W[base + q] = __dmul_rn(__dmul_rn(nd[3][i], nd[4][j]), nd[5][k]);
+        }
+        __syncwarp();
     }
 }
 
@@ -540,41 +534,44 @@ int tagi_mesh_points(const double *cellX, const double *cellY, const double *cel
     }
     for (int i = p1; i < MESH_MAX_P1; i++) t.u[i] = t.w[i] = 0.0;
     cudaStream_t s = (cudaStream_t)stream;
-    const long npc = (long)numCoarsePoints;
-    int g = grid_for(npc);
-    if (g > 152 * 64) g = 152 * 64;
-    launch(mesh_coarse_points, g, MT, 0, s, cellX, cellY, cellZ, cellDX, cellDY, cellDZ, npc, p1, t, X, Y, Z, W);
+    auto warp_grid = [](long nsubcells) {
+        long g = (nsubcells + PW - 1) / PW;
+        return (int)(g < 1 ? 1 : (g > 152L * 32 ? 152L * 32 : g));
+    };
+    launch(mesh_points_warp, warp_grid(numCells), PW * 32, 0, s, cellX, cellY, cellZ, cellDX, cellDY, cellDZ,
+           (const int *)nullptr, (const int *)nullptr, numCells, (long)numCells, p1, t, X, Y, Z, W);
     TAGI_LAUNCH_CHECK();
     if (!fine) return TAGI_OK;
     Arena tmp;
     tmp.stream = s;
     int rc = TAGI_OK;
     do {
-        int *sub = nullptr, *off = nullptr, *err = nullptr;
-        if ((rc = tmp.alloc(&sub, numCells)) || (rc = tmp.alloc(&off, numCells + 1)) || (rc = tmp.alloc(&err, 1)))
+        int *sub = nullptr, *nsub = nullptr, *off = nullptr, *err = nullptr;
+        if ((rc = tmp.alloc(&sub, numCells)) || (rc = tmp.alloc(&nsub, numCells)) ||
+            (rc = tmp.alloc(&off, numCells + 1)) || (rc = tmp.alloc(&err, 1)))
             break;
         if (cudaMemsetAsync(err, 0, sizeof(int), s) != cudaSuccess) {
             rc = set_error(TAGI_ERR_CUDA, "mesh memset failed");
             break;
         }
-        launch(mesh_fine_counts, grid_for(numCells), MT, 0, s, ptsPerCellFine, numCells, p3, sub, err);
-        if ((rc = exclusive_scan(ptsPerCellFine, off, numCells, off + numCells, tmp, s))) break;
+        launch(mesh_fine_counts, grid_for(numCells), MT, 0, s, ptsPerCellFine, numCells, p3, sub, nsub, err);
+        if ((rc = exclusive_scan(nsub, off, numCells, off + numCells, tmp, s))) break;
         int h[2] = {0, 0};
         if ((rc = read_ints(off + numCells, &h[0], 1, s)) || (rc = read_ints(err, &h[1], 1, s))) break;
         if (h[1]) {
             rc = set_error(TAGI_ERR_ARG, "a fine cell holds a point count other than 1, 8, 27 or 64 x (order+1)^3");
             break;
         }
-        if ((long long)h[0] != numFinePoints) {
-            rc = set_error(TAGI_ERR_ARG, "ptsPerCellFine sums to %d, numFinePoints is %lld", h[0], numFinePoints);
+        const long long fine_pts = (long long)h[0] * p3;
+        if (fine_pts != numFinePoints) {
+            rc = set_error(TAGI_ERR_ARG, "ptsPerCellFine sums to %lld, numFinePoints is %lld", fine_pts,
+                           numFinePoints);
             break;
         }
         if (numFinePoints == 0) break;
-        int gf = grid_for((long)numFinePoints);
-        if (gf > 152 * 64) gf = 152 * 64;
-        launch(mesh_fine_points, gf, MT, 0, s, cellX, cellY, cellZ, cellDX, cellDY, cellDZ, off, sub, numCells,
-               (long)numFinePoints, p1, t, Xf, Yf, Zf, Wf);
-        if (cudaGetLastError() != cudaSuccess) rc = set_error(TAGI_ERR_CUDA, "mesh_fine_points launch failed");
+        launch(mesh_points_warp, warp_grid(h[0]), PW * 32, 0, s, cellX, cellY, cellZ, cellDX, cellDY, cellDZ,
+               (const int *)off, (const int *)sub, numCells, (long)h[0], p1, t, Xf, Yf, Zf, Wf);
+        if (cudaGetLastError() != cudaSuccess) rc = set_error(TAGI_ERR_CUDA, "mesh_points_warp launch failed");
     } while (0);
     tmp.release();
     return rc;
