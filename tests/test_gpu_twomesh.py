@@ -5,9 +5,11 @@ Checked against the oracle's restatement (oracle/gi_oracle.py
 two_mesh_correction: the oracle's interpolation and FP64 treecode with the
 same tree and list rules, numpy for the rest).  Tolerances: FP64 device path
 agrees to rounding (1e-10 relative on V_H and E_H, 1e-9 Ha on dE); the mixed
-path within 1e-6 relative (V_H) and 1e-6 Ha (dE).  Known answer: the Hartree
-potential of a normalized Gaussian is erf(sqrt(a) r)/r; with the fine mesh as
-sources its error is below the coarse-only convolution's.
+path within 1e-6 relative (V_H), and dE within the shift that a 1e-6
+relative error of the convolution can cause (bound computed in the test).
+Known answer: the Hartree potential of a normalized Gaussian is
+erf(sqrt(a) r)/r; with the fine mesh as sources its error is below the
+coarse-only convolution's.
 """
 import importlib
 import math
@@ -73,7 +75,15 @@ def test_mixed_matches_oracle(setup):
     out = c.correct(psi, eps, rho)
     vh = out["vhartree"].cpu().numpy()
     assert np.linalg.norm(vh - vh_ref) / np.linalg.norm(vh_ref) <= 1e-6
-    assert np.max(np.abs(out["deltaE"] - dE_ref)) <= 1e-6
+    # dE = -<psi V (psi - c)>_W / <c^2>_W with c = psiNew carrying <= 1e-6
+    # relative error: dE moves by up to 1e-6 (|<psi V c>_W| + 2 |dE| <c^2>_W) / <c^2>_W
+    W = h["W"]
+    conv = out["psi_new"].cpu().numpy()
+    veff = out["veff"].cpu().numpy()
+    for mm in range(len(eps)):
+        c2 = np.sum(W * conv[mm] ** 2)
+        bound = 1e-6 * (abs(np.sum(W * psi[mm] * veff * conv[mm])) + 2 * abs(dE_ref[mm]) * c2) / c2
+        assert abs(out["deltaE"][mm] - dE_ref[mm]) <= bound, (mm, bound)
     c.close()
 
 
