@@ -14,7 +14,7 @@ convolutions/s over all ranks.  ``e2e`` = the same through the C ABI
 device allocation and the device->host result copy are inside the timing.
 
   python bench.py [--gpus N] [--steps K] [--warmup W] [--impl gb300|reference]
-                  [--workload hartree|orbitals|uneven]
+                  [--workload hartree|orbitals|uneven|scf|mesh|twomesh]
 
 ``--workload uneven``: six independent synthetic systems (50k .. 2.5M points,
 4/8/8/16/32/64 orbitals, Yukawa with subtraction, k_i ~ U[0.4, 3]) convolved
@@ -24,6 +24,10 @@ kernel shape chosen by the autotuner (untimed).  One step = one replay: one
 Green-iteration sweep's convolutions (plans reused, as Green iteration reuses
 them).  Compared with the plain path: one FP64 tagi_treecode_dev call per
 orbital (tree + convolution each, reference parameters: leaves 500).
+
+``--workload mesh``: the ring molecule's two-level mesh built on the device
+(refinement + coarse and fine points); ``--workload twomesh``: the two-mesh
+eigenvalue correction of 21 orbitals on that mesh.
 
 ``--impl reference`` times the CPU FP64 restatement of the same treecode (the
 reference's BaryTree is not available) on the host cores, on a bounded sample
@@ -59,7 +63,7 @@ def parse():
     ap.add_argument("--steps", type=int, default=5)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
-    ap.add_argument("--workload", default="hartree", choices=["hartree", "orbitals", "uneven", "scf", "mesh"])
+    ap.add_argument("--workload", default="hartree", choices=["hartree", "orbitals", "uneven", "scf", "mesh", "twomesh"])
     ap.add_argument("--scf-points", type=int, default=3_000_000, help="scf workload: mesh points")
     ap.add_argument("--scf-max-iter", type=int, default=60)
     ap.add_argument("--scf-orbitals", type=int, default=21, help="scf workload: orbitals (21 occupied)")
@@ -847,12 +851,169 @@ def mesh_arm(args):
     return 0
 
 
+def cpu_two_mesh_sample(tab, pts, nuclei, target_seconds, threads):
+    """Oracle cost of one orbital's two-mesh correction on a mesh: the FP64
+    plan (coarse targets, fine sources, theta 0.55, degree 9) and upward pass
+    timed in full, the Yukawa field on a sample of target batches sized to
+    ~target_seconds, extrapolated by pair count.  Returns (seconds, info)."""
+    from oracle import oracle as O
+    O.build()
+    X, Y, Z, W, Xf, Yf, Zf, Wf = pts
+    t0 = time.perf_counter()
+    plan = O.Plan(X, Y, Z, Xf, Yf, Zf, Wf, THETA - 0.15, DEGREE + 2, 2000, 2000, 1.0)
+    t_plan = time.perf_counter() - t0
+    L_ = plan.lists()
+    st, tt = plan.tree(0), plan.tree(1)
+    nb = plan.n_batches
+    bsz = tt["end"][L_["batch_node"]] - tt["begin"][L_["batch_node"]]
+    src_len = st["end"] - st["begin"]
+    ncnt = np.array([src_len[L_["near_list"][L_["near_off"][b]:L_["near_off"][b + 1]]].sum() for b in range(nb)])
+    pairs_b = bsz * (ncnt + np.diff(L_["far_off"]) * plan.P)
+    R = nuclei[0]
+    fc = np.exp(-np.sqrt((X - R[0]) ** 2 + (Y - R[1]) ** 2 + (Z - R[2]) ** 2))
+    ff = np.exp(-np.sqrt((Xf - R[0]) ** 2 + (Yf - R[1]) ** 2 + (Zf - R[2]) ** 2))
+    order = np.random.default_rng(17).permutation(nb)
+    sel = np.sort(order[:4])
+    _, (t_up, t_f), (pn, pf) = O.convolve_batches(plan, fc, ff, Wf, 2, [1.0], 2, sel, threads)
+    want = (pn + pf) / max(t_f, 1e-9) * target_seconds
+    nsel = int(np.clip(np.searchsorted(np.cumsum(pairs_b[order]), want) + 1, 4, nb))
+    sel = np.sort(order[:nsel])
+    _, (t_up, t_f), (pn, pf) = O.convolve_batches(plan, fc, ff, Wf, 2, [1.0], 2, sel, threads)
+    frac = (pn + pf) / pairs_b.sum()
+    return t_plan + t_up + t_f / frac, dict(plan_s=t_plan, upward_s=t_up, batches=nsel, of_batches=nb,
+                                            pair_fraction=float(frac), pairs_per_s=(pn + pf) / t_f)
+
+
+def twomesh_arm(args):
+    """Two-mesh eigenvalue correction (twomesh.TwoMeshCorrection) of the ring
+    molecule's 21 atom-centred orbitals on its device-built two-level mesh
+    (MESH_CFG: 2.61M coarse, 14.3M fine points).  One step = one whole
+    correction: interpolations, the Hartree convolution and the 21 Yukawa
+    convolutions (one batched launch per field pass) with coarse targets and
+    fine sources at theta 0.55, degree 9, exchange, Harrison update; the plan
+    is built once (untimed), as the reference's correction reuses one tree
+    per call.  value = orbitals corrected per second."""
+    import torch
+    from types import SimpleNamespace
+    ws, rank, local = dist_env()
+    torch.cuda.set_device(local)
+    pkg = importlib.import_module(PKG)
+    M = importlib.import_module(PKG + ".mesh")
+    T = importlib.import_module(PKG + ".twomesh")
+    nat = pkg._native
+    L = nat.lib()
+    c = MESH_CFG
+    nuclei, charges = pkg.synthetic.ring_molecule()
+
+    def setup(h):
+        m = M.build_mesh(c["XL"], c["max_side"], nuclei, c["order"], h, c["H"], c["r"], c["level"])
+        hx = SimpleNamespace(x=m.X.cpu().numpy(), y=m.Y.cpu().numpy(), z=m.Z.cpu().numpy())
+        psi, eps = ring_guess(hx, nuclei, charges, 21)
+        w = m.W.cpu().numpy()
+        psi /= np.sqrt((psi * psi * w).sum(1))[:, None]
+        rho = 2.0 * (psi * psi).sum(0)
+        corr = T.TwoMeshCorrection(m.X, m.Y, m.Z, m.W, m.Xf, m.Yf, m.Zf, m.Wf, m.PtsPerCellCoarse,
+                                   m.PtsPerCellFine, c["order"], nuclei, charges, theta=THETA, degree=DEGREE,
+                                   source_leaf=2000, target_leaf=2000, precision="mixed")
+        return m, corr, psi, eps, rho
+
+    m, corr, psi, eps, rho = setup(c["h"])
+    psi_d = torch.as_tensor(psi, device="cuda")
+    rho_d = torch.as_tensor(rho, device="cuda")
+    for _ in range(max(args.warmup, 1)):
+        out = corr.correct(psi_d, eps, rho_d, n_electrons=42.0)
+    corr.stream.synchronize()
+    prof_ms = np.zeros(7)
+    prof_n = np.zeros(7, dtype=np.int64)
+    prof_np = prof_n.ctypes.data_as(ctypes.POINTER(ctypes.c_longlong))
+    L.tagi_profile(1)
+    L.tagi_profile_read(nat.dptr(prof_ms), prof_np, 7)
+    ev = [torch.cuda.Event(enable_timing=True) for _ in range(2)]
+    n0 = L.tagi_launch_count()
+    with ClockSampler(local) as clocks:
+        ev[0].record(corr.stream)
+        for _ in range(args.steps):
+            out = corr.correct(psi_d, eps, rho_d, n_electrons=42.0)
+        ev[1].record(corr.stream)
+        corr.stream.synchronize()
+    launches = int(L.tagi_launch_count() - n0)
+    L.tagi_profile_read(nat.dptr(prof_ms), prof_np, 7)
+    L.tagi_profile(0)
+    ms = ev[0].elapsed_time(ev[1]) / args.steps
+    info = corr.plan.info()
+    # dominant kernel: the near field (1 Hartree + 21 Yukawa orbitals per step)
+    near_pairs = (info["near_pairs"] - info["near_close_pairs"]) * 22 * args.steps
+    far_pairs = info["far_pairs"] * 22 * args.steps
+    dominant = "near" if prof_ms[3] >= prof_ms[4] else "far"
+    k_ms = prof_ms[3] if dominant == "near" else prof_ms[4]
+    k_pairs = near_pairs if dominant == "near" else far_pairs
+    peak = ctypes.c_double()
+    nat.check(L.tagi_pair_peak(2, 2, 0 if dominant == "near" else 1, 1.0, ctypes.byref(peak),
+                               ctypes.c_void_p(torch.cuda.current_stream().cuda_stream)))
+    achieved = k_pairs / (k_ms * 1e-3)
+    # e2e: host orbitals and density in, corrected eigenvalues out
+    e2e_ms = []
+    for _ in range(args.steps):
+        a = time.perf_counter()
+        o = corr.correct(psi, eps, rho, n_electrons=42.0)
+        e2e_ms.append((time.perf_counter() - a) * 1e3)
+    line = {"metric": "two-mesh eigenvalue corrections/s (orbitals)", "value": 21 / (ms * 1e-3),
+            "unit": "orbitals/s", "n_gpus": 1, "steps": args.steps, "warmup": max(args.warmup, 1),
+            "ms_per_step": ms, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+            "dtype": "f32+f64", "data": "synthetic ring molecule (12 nuclei), atom-centred guess orbitals",
+            "config": {"workload": "ring_two_mesh_correction_21_orbitals", "coarse_points": int(m.n),
+                       "fine_points": int(m.Xf.numel()), "theta": THETA - 0.15, "degree": DEGREE + 2,
+                       "leaf": [2000, 2000], "precision": "mixed",
+                       "l2": "inputs (2.6M x 21 orbitals, 14.3M-point fine mesh) larger than L2",
+                       "eigenvalue_corrections": [float(v) for v in out["deltaE"]]},
+            "phase_ms_per_step": {k: float(prof_ms[i]) / args.steps for i, k in
+                                  enumerate(("tree", "lists", "upward", "near", "far", "glue", "near_close"))},
+            "roofline": {"bound": "mufu", "kernel": f"{dominant}_mixed (yukawa/coulomb ss)",
+                         "achieved": achieved / 1e9, "peak": peak.value / 1e9, "unit": "Gpair/s",
+                         "frac": achieved / peak.value, "traffic": None,
+                         "peak_source": "tagi_pair_peak (Yukawa SS pair arithmetic, measured live)"},
+            "e2e": {"value": 21 / (statistics.median(e2e_ms) * 1e-3), "unit": "orbitals/s",
+                    "h2d_bytes_per_step": int(psi.nbytes + rho.nbytes), "d2h_bytes_per_step": 8 * 21},
+            "clocks": clocks.summary(), "gpu_launches": launches}
+    corr.close()
+    del corr, psi_d, rho_d, out, m
+    torch.cuda.empty_cache()
+    if not args.no_cpu_baseline:
+        # same construction at h = 3 (320k coarse / 721k fine points): GPU and oracle side by side
+        hs = 3.0
+        ms_small, corr_s, psi_s, eps_s, rho_s = setup(hs)
+        corr_s.correct(psi_s, eps_s, rho_s)
+        a = torch.cuda.Event(enable_timing=True)
+        b = torch.cuda.Event(enable_timing=True)
+        a.record(corr_s.stream)
+        corr_s.correct(psi_s, eps_s, rho_s)
+        b.record(corr_s.stream)
+        corr_s.stream.synchronize()
+        gpu_small = 21 / (a.elapsed_time(b) * 1e-3)
+        from oracle import mesh_oracle as MO
+        tab, pts = MO.build(c["XL"], c["max_side"], nuclei, c["order"], hs, c["H"], c["r"], c["level"])
+        threads = os.cpu_count() or 1
+        secs, inf = cpu_two_mesh_sample(tab, pts, nuclei, args.cpu_seconds, threads)
+        line["cpu_baseline"] = {
+            "value": 1.0 / secs, "unit": "orbitals/s", "cores": threads, "kind": "port",
+            "sample": (f"oracle FP64 correction of one orbital on the same construction at h = {hs} "
+                       f"({len(pts[0])} coarse / {len(pts[4])} fine points): plan + upward timed in full, "
+                       f"Yukawa field on {inf['batches']} of {inf['of_batches']} batches "
+                       f"({inf['pair_fraction']:.3f} of the pairs), extrapolated by pair count"),
+            "gpu_same_mesh_orbitals_per_s": gpu_small}
+        corr_s.close()
+    print(json.dumps(line), flush=True)
+    return 0
+
+
 def main():
     args = parse()
     if args.impl == "reference":
         return reference_arm(args)
     if args.workload == "mesh":
         return mesh_arm(args)
+    if args.workload == "twomesh":
+        return twomesh_arm(args)
     if args.workload == "uneven":
         return uneven_arm(args)
     if args.workload == "scf":

@@ -259,13 +259,13 @@ __global__ void __launch_bounds__(PW * 32) mesh_points_warp(const double *__rest
                                                             const double *__restrict__ dz,
                                                             const int *__restrict__ sub_off,
                                                             const int *__restrict__ sub, int ncells,
-                                                            long nsubcells, int p1,
-                                                            const __grid_constant__ Tables t,
+                                                            long nsubcells, int p1, unsigned m1,
+                                                            unsigned m2, const __grid_constant__ Tables t,
                                                             double *__restrict__ X, double *__restrict__ Y,
                                                             double *__restrict__ Z, double *__restrict__ W) {
     __shared__ double sh[PW][6][MESH_MAX_P1];
     const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
-    const int p2 = p1 * p1, p3 = p2 * p1;
+    const int p3 = p1 * p1 * p1;
     double(*nd)[MESH_MAX_P1] = sh[wid];
     for (long s = (long)blockIdx.x * PW + wid; s < nsubcells; s += (long)gridDim.x * PW) {
         int c = (int)s, m = 1, child = 0;
@@ -297,7 +297,12 @@ __global__ void __launch_bounds__(PW * 32) mesh_points_warp(const double *__rest
         __syncwarp();
         const long base = s * p3;
         for (int q = lane; q < p3; q += 32) {
-            const int i = q / p2, j = (q / p1) % p1, k = q % p1;
+            // i = q / p2, j = (q / p1) % p1, k = q % p1 by high multiplies with
+            // m = ceil(2^32 / d): exact for q d < 2^32 (q < 4096, d <= 256)
+            const unsigned uq = (unsigned)q, tq = __umulhi(uq, m1);
+            const int i = (int)__umulhi(uq, m2);
+            const int j = (int)(tq - __umulhi(tq, m1) * (unsigned)p1);
+            const int k = (int)(uq - tq * (unsigned)p1);
             X[base + q] = nd[0][i];
             Y[base + q] = nd[1][j];
             Z[base + q] = nd[2][k];
@@ -534,22 +539,27 @@ int tagi_mesh_points(const double *cellX, const double *cellY, const double *cel
     }
     for (int i = p1; i < MESH_MAX_P1; i++) t.u[i] = t.w[i] = 0.0;
     cudaStream_t s = (cudaStream_t)stream;
+    const int p2 = p1 * p1;
+    const unsigned m1 = p1 > 1 ? (unsigned)((0x100000000ULL + p1 - 1) / p1) : 0u;
+    const unsigned m2 = p2 > 1 ? (unsigned)((0x100000000ULL + p2 - 1) / p2) : 0u;
     auto warp_grid = [](long nsubcells) {
         long g = (nsubcells + PW - 1) / PW;
         return (int)(g < 1 ? 1 : (g > 152L * 32 ? 152L * 32 : g));
     };
     launch(mesh_points_warp, warp_grid(numCells), PW * 32, 0, s, cellX, cellY, cellZ, cellDX, cellDY, cellDZ,
-           (const int *)nullptr, (const int *)nullptr, numCells, (long)numCells, p1, t, X, Y, Z, W);
+           (const int *)nullptr, (const int *)nullptr, numCells, (long)numCells, p1, m1, m2, t, X, Y, Z, W);
     TAGI_LAUNCH_CHECK();
     if (!fine) return TAGI_OK;
     Arena tmp;
     tmp.stream = s;
     int rc = TAGI_OK;
     do {
-        int *sub = nullptr, *nsub = nullptr, *off = nullptr, *err = nullptr;
+        // off[numCells] receives the sub-cell total, off[numCells + 1] the error flag
+        int *sub = nullptr, *nsub = nullptr, *off = nullptr;
         if ((rc = tmp.alloc(&sub, numCells)) || (rc = tmp.alloc(&nsub, numCells)) ||
-            (rc = tmp.alloc(&off, numCells + 1)) || (rc = tmp.alloc(&err, 1)))
+            (rc = tmp.alloc(&off, numCells + 2)))
             break;
+        int *err = off + numCells + 1;
         if (cudaMemsetAsync(err, 0, sizeof(int), s) != cudaSuccess) {
             rc = set_error(TAGI_ERR_CUDA, "mesh memset failed");
             break;
@@ -557,7 +567,7 @@ int tagi_mesh_points(const double *cellX, const double *cellY, const double *cel
         launch(mesh_fine_counts, grid_for(numCells), MT, 0, s, ptsPerCellFine, numCells, p3, sub, nsub, err);
         if ((rc = exclusive_scan(nsub, off, numCells, off + numCells, tmp, s))) break;
         int h[2] = {0, 0};
-        if ((rc = read_ints(off + numCells, &h[0], 1, s)) || (rc = read_ints(err, &h[1], 1, s))) break;
+        if ((rc = read_ints(off + numCells, h, 2, s))) break;
         if (h[1]) {
             rc = set_error(TAGI_ERR_ARG, "a fine cell holds a point count other than 1, 8, 27 or 64 x (order+1)^3");
             break;
@@ -570,7 +580,7 @@ int tagi_mesh_points(const double *cellX, const double *cellY, const double *cel
         }
         if (numFinePoints == 0) break;
         launch(mesh_points_warp, warp_grid(h[0]), PW * 32, 0, s, cellX, cellY, cellZ, cellDX, cellDY, cellDZ,
-               (const int *)off, (const int *)sub, numCells, (long)h[0], p1, t, Xf, Yf, Zf, Wf);
+               (const int *)off, (const int *)sub, numCells, (long)h[0], p1, m1, m2, t, Xf, Yf, Zf, Wf);
         if (cudaGetLastError() != cudaSuccess) rc = set_error(TAGI_ERR_CUDA, "mesh_points_warp launch failed");
     } while (0);
     tmp.release();
