@@ -226,9 +226,72 @@ def cpu_treecode_sample(wl, target_seconds, threads, leaf=None):
                          pairs_per_s=(pn + pf) / t_f, total_pairs=float(total_pairs))
 
 
+def reference_arm_mesh(args):
+    """The oracle's restatement of the reference's mesh construction, whole mesh per step."""
+    from oracle import mesh_oracle as MO
+    pkg = importlib.import_module(PKG)
+    c = MESH_CFG
+    nuclei, _ = pkg.synthetic.ring_molecule()
+    secs, n = [], 0
+    for k in range(args.warmup + args.steps):
+        a = time.perf_counter()
+        base = MO.base_cells(c["XL"], c["XL"], c["XL"], c["max_side"])
+        tab = MO.cell_table(MO.refine(base, nuclei, c["h"], c["H"], c["r"], c["level"]), c["order"])
+        pts = MO.points(tab, c["order"])
+        if k >= args.warmup:
+            secs.append(time.perf_counter() - a)
+        n = len(pts[0]) + len(pts[4])
+    value = n / float(np.mean(secs))
+    unit = "points/s"
+    return {"metric": "mesh points/s (two-level first-kind mesh, refinement + points)", "value": value,
+            "unit": unit, "ms_per_step": float(np.mean(secs)) * 1e3, "dtype": "f64",
+            "config": {"workload": "ring_two_level_mesh", **c},
+            "cpu_baseline": {"value": value, "unit": unit, "cores": 1, "kind": "port",
+                             "sample": "whole mesh per step (Python recursion, numpy per cell)"},
+            "e2e": {"value": value, "unit": unit, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+
+
+def reference_arm_twomesh(args):
+    """Oracle FP64 two-mesh correction cost per orbital on the h = 3 construction."""
+    from oracle import mesh_oracle as MO
+    pkg = importlib.import_module(PKG)
+    c = MESH_CFG
+    nuclei, _ = pkg.synthetic.ring_molecule()
+    tab, pts = MO.build(c["XL"], c["max_side"], nuclei, c["order"], 3.0, c["H"], c["r"], c["level"])
+    threads = os.cpu_count() or 1
+    per_step = max(2.0, args.cpu_seconds / 4)
+    secs = []
+    for k in range(args.warmup + args.steps):
+        s, info = cpu_two_mesh_sample(tab, pts, nuclei, per_step, threads)
+        if k >= args.warmup:
+            secs.append(s)
+    value = 1.0 / float(np.mean(secs))
+    unit = "orbitals/s"
+    sample = (f"oracle FP64 correction of one orbital at h = 3 ({len(pts[0])} coarse / {len(pts[4])} fine "
+              f"points): plan + upward in full, Yukawa field on {info['batches']} of {info['of_batches']} "
+              "batches, extrapolated by pair count")
+    return {"metric": "two-mesh eigenvalue corrections/s (orbitals)", "value": value, "unit": unit,
+            "ms_per_step": float(np.mean(secs)) * 1e3, "dtype": "f64",
+            "config": {"workload": "ring_two_mesh_correction_h3", "coarse_points": len(pts[0]),
+                       "fine_points": len(pts[4]), "theta": THETA - 0.15, "degree": DEGREE + 2},
+            "cpu_baseline": {"value": value, "unit": unit, "cores": threads, "kind": "port", "sample": sample},
+            "e2e": {"value": value, "unit": unit, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+
+
 def reference_arm(args):
     ws, rank, local = dist_env()
     if rank != 0:
+        return 0
+    if args.workload in ("mesh", "twomesh"):
+        body = (reference_arm_mesh if args.workload == "mesh" else reference_arm_twomesh)(args)
+        line = {"impl": "reference", "n_gpus": 0, "steps": args.steps, "warmup": args.warmup,
+                "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+                "data": "synthetic ring molecule (seeded)", **body}
+        print(json.dumps(line), flush=True)
+        return 0
+    if args.workload == "scf":
+        print(json.dumps({"impl": "reference", "unavailable": "the reference SCF needs its atomic data files "
+                          "and BaryTree, neither of which is present"}), flush=True)
         return 0
     wl = make_workload(args.workload)
     threads = os.cpu_count() or 1
