@@ -74,3 +74,64 @@ def test_argument_errors_before_any_device_work(native):
     rc = L.tagi_BaryTreeInterface_ex(*common, 2, 1, native.dptr(bad_k), 2, 1, 1, 0.7, 7, 10, 10, 1.0,
                                      -1.0, 0, 1)
     assert rc == native.TAGI_ERR_ARG
+
+
+def declared_arities():
+    """{name: parameter count} from include/tagi_gb300.h."""
+    src = open(os.path.join(ROOT, "include", "tagi_gb300.h")).read()
+    src = re.sub(r"/\*.*?\*/", "", src, flags=re.S)
+    out = {}
+    for m in re.finditer(r"^\s*(?:void|int|long long|const char \*|double)\s*\*?\s*(\w+)\s*\(([^)]*)\)\s*;",
+                         src, flags=re.M | re.S):
+        params = m.group(2).strip()
+        out[m.group(1)] = 0 if params in ("", "void") else params.count(",") + 1
+    return out
+
+
+def test_binding_arities_match_header(native):
+    """Every ctypes signature has as many parameters as the header declares."""
+    ar = declared_arities()
+    assert set(ar) == set(native.SIGNATURES)
+    bad = {n: (ar[n], len(native.SIGNATURES[n][1])) for n in ar if ar[n] != len(native.SIGNATURES[n][1])}
+    assert not bad, bad
+
+
+def test_mesh_entry_points_refuse_bad_arguments_on_the_host(native):
+    """tagi_mesh_refine / tagi_mesh_points validate before touching the device."""
+    L = native.lib()
+    base = np.array([[-1.0, 1.0, -1.0, 1.0, -1.0, 1.0]])
+    atoms = np.array([[0.1, 0.2, 0.3]])
+    n, nc, nf = ctypes.c_int(-7), ctypes.c_longlong(0), ctypes.c_longlong(0)
+    null8 = [None] * 8
+
+    def refine(numBase=1, order=3, level=-2.0, minDepth=0, maxDepth=16, h=1.0, numCells=True):
+        return L.tagi_mesh_refine(native.dptr(base), numBase, native.dptr(atoms), 1, order, h, 4.0, 1.0, level,
+                                  minDepth, maxDepth, *null8, 0, ctypes.byref(n) if numCells else None,
+                                  ctypes.byref(nc), ctypes.byref(nf), None)
+
+    assert refine(numCells=False) == native.TAGI_ERR_ARG
+    assert refine(numBase=0) == native.TAGI_ERR_ARG and n.value == 0
+    assert refine(numBase=1 << 17) == native.TAGI_ERR_ARG
+    assert refine(order=16) == native.TAGI_ERR_UNSUPPORTED
+    assert refine(level=-5.0) == native.TAGI_ERR_UNSUPPORTED
+    assert b"children" in L.tagi_last_error_message()
+    assert refine(maxDepth=17) == native.TAGI_ERR_ARG
+    assert refine(minDepth=-1) == native.TAGI_ERR_ARG
+    assert refine(h=float("nan")) == native.TAGI_ERR_ARG
+    c = np.zeros(4)
+    cp = native.dptr(c)
+    dp = ctypes.POINTER(ctypes.c_double)
+    u = np.zeros(4)
+
+    def points(numCells=1, order=3, ncoarse=64, tables=(None, None), fine=False, nfine=0):
+        f = [cp] * 4 if fine else [None] * 4
+        return L.tagi_mesh_points(cp, cp, cp, cp, cp, cp, None, numCells, order, tables[0], tables[1],
+                                  cp, cp, cp, cp, ncoarse, *f, nfine, None)
+
+    assert points(numCells=-1) == native.TAGI_ERR_ARG
+    assert points(order=16) == native.TAGI_ERR_UNSUPPORTED
+    assert points(ncoarse=63) == native.TAGI_ERR_ARG
+    assert points(numCells=0, ncoarse=0) == native.TAGI_OK
+    assert points(fine=True) == native.TAGI_ERR_ARG          # fine arrays without ptsPerCellFine
+    assert points(tables=(u.ctypes.data_as(dp), None)) == native.TAGI_ERR_ARG
+    L.tagi_clear_error()
