@@ -120,3 +120,58 @@ def test_two_mesh_oracle_identity_mesh(oracle):
     c = plan.convolve(-2 * psi[0] * veff, -2 * psi[0] * veff, W, 2, [1.0], 2) / (4 * math.pi)
     d = -np.sum(W * psi[0] * veff * (psi[0] - c)) / np.sum(W * c * c)
     assert abs(dE[0] - d) <= 1e-12 * max(1.0, abs(d))
+
+
+def _level_sync_order(base, atoms, h, H, r, level, min_depth=0, depth_bits=16):
+    """The device refinement's ordering scheme, restated: cells emitted level by
+    level, each carrying a path key (base index << 48 | 3-bit child digit per
+    level), leaves sorted by key at the end."""
+    atoms = [tuple(a) for a in np.asarray(atoms, np.float64).reshape(-1, 3)]
+    cells = [tuple(map(float, b)) for b in base]
+    keys = [i << 48 for i in range(len(cells))]
+    leaves, depth = [], 0
+    while cells:
+        nxt, nkeys = [], []
+        for c, k in zip(cells, keys):
+            div, fine = (True, 1) if depth < min_depth else MO.divide_rule(c, atoms, h, H, r, level)
+            if not div:
+                leaves.append((k, c, fine))
+                continue
+            xb = [c[0], (c[1] + c[0]) / 2, c[1]]
+            yb = [c[2], (c[3] + c[2]) / 2, c[3]]
+            zb = [c[4], (c[5] + c[4]) / 2, c[5]]
+            for q in range(8):
+                i, j, kk = q >> 2, (q >> 1) & 1, q & 1
+                nxt.append((xb[i], xb[i + 1], yb[j], yb[j + 1], zb[kk], zb[kk + 1]))
+                nkeys.append(k | (q << (3 * (depth_bits - 1 - depth))))
+        cells, keys, depth = nxt, nkeys, depth + 1
+    leaves.sort(key=lambda t: t[0])
+    return [(c, f) for _, c, f in leaves]
+
+
+@pytest.mark.parametrize("level,min_depth", [(-2.0, 0), (0.0, 2), (2.0, 0)])
+def test_path_key_order_is_depth_first(syn, level, min_depth):
+    """Sorting leaves by padded path key gives the reference's uniqueID
+    (depth-first, x-major) order: a leaf is never a prefix of another leaf."""
+    nuclei, _ = syn.ring_molecule()
+    base = MO.base_cells(12.0, 12.0, 12.0, 4.0)
+    a = _level_sync_order(base, nuclei, 1.5, 4.0, 1.5, level, min_depth)
+    b = MO.refine(base, nuclei, 1.5, 4.0, 1.5, level, min_depth)
+    assert len(a) == len(b)
+    assert all(x[0] == tuple(y[0]) and x[1] == y[1] for x, y in zip(a, b))
+
+
+def test_high_multiply_index_split_is_exact():
+    """The points kernel splits q = i p^2 + j p + k with high multiplies by
+    ceil(2^32 / d) (d = p, p^2; 0 for d = 1, where q is always 0): exact for
+    every order 0..15 and every q < (order+1)^3."""
+    for p1 in range(1, 17):
+        p2, p3 = p1 * p1, p1 * p1 * p1
+        m1 = -(-(1 << 32) // p1) if p1 > 1 else 0
+        m2 = -(-(1 << 32) // p2) if p2 > 1 else 0
+        assert m1 < (1 << 32) and m2 < (1 << 32)
+        q = np.arange(p3, dtype=np.uint64)
+        hi = lambda a, m: (a * np.uint64(m)) >> np.uint64(32)
+        t = hi(q, m1)
+        i, j, k = hi(q, m2), t - hi(t, m1) * np.uint64(p1), q - t * np.uint64(p1)
+        assert np.array_equal(i, q // p2) and np.array_equal(j, (q // p1) % p1) and np.array_equal(k, q % p1)
