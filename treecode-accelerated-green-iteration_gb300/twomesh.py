@@ -107,6 +107,7 @@ class TwoMeshCorrection:
     def hartree(self, rho):
         """V_H on the coarse mesh from RHO (coarse) and its fine interpolant."""
         rho = _t(rho)
+        self.stream.wait_stream(torch.cuda.current_stream())  # inputs made on the caller's stream
         with torch.cuda.stream(self.stream):
             rho_f = self.interpolate(rho)
             vh = self.plan.convolve(rho, rho_f, Kernel.COULOMB, [self.alpha], Singularity.SUBTRACTION,
@@ -129,6 +130,7 @@ class TwoMeshCorrection:
             raise ValueError("eigenvalues must be negative (k = sqrt(-2 eps))")
         rho = _t(rho)
         f64 = dict(dtype=torch.float64, device="cuda")
+        self.stream.wait_stream(torch.cuda.current_stream())  # inputs made on the caller's stream
         with torch.cuda.stream(self.stream):
             vh, _ = self.hartree(rho)
             vx = torch.empty(self.n, **f64)
