@@ -100,6 +100,8 @@ def refine_cells(base, atoms, order, h, H, r, level, min_depth=0, max_depth=16, 
     atoms_d = torch.as_tensor(np.asarray(atoms, np.float64).reshape(-1, 3) if not torch.is_tensor(atoms) else atoms,
                               dtype=torch.float64, device=device).contiguous()
     nb, na = base_d.shape[0], atoms_d.shape[0]
+    if stream is not None:
+        stream.wait_stream(torch.cuda.current_stream())  # base_d / atoms_d were made there
     ncell, ncp, nfp = ctypes.c_int(0), ctypes.c_longlong(0), ctypes.c_longlong(0)
     args = (_dev(base_d, "base"), nb, _dev(atoms_d, "atoms") if na else ctypes.c_void_p(0), na, int(order),
             float(h), float(H), float(r), float(level), int(min_depth), int(max_depth))
@@ -129,6 +131,8 @@ def mesh_points(cells, ppc_f, order, num_fine=None, tables=None, device="cuda", 
     C = [torch.empty(n * p3, **f64) for _ in range(4)]
     F = [torch.empty(int(num_fine), **f64) for _ in range(4)] if num_fine is not None else None
     dp = ctypes.POINTER(ctypes.c_double)
+    if stream is not None:
+        stream.wait_stream(torch.cuda.current_stream())  # output buffers were made there
     cargs = [_dev(c, "cell") for c in cells]
     fine_args = [_dev(a, "fine") for a in F] if F is not None else [ctypes.c_void_p(0)] * 4
     _native.check(_native.lib().tagi_mesh_points(
