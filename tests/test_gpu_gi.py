@@ -213,3 +213,64 @@ def test_orbital_anderson_mixing(dev, gi_mod, syn):
     assert checked and res < 1e-6
     g.close()
     plan.close()
+
+
+def test_two_green_iterations_on_their_own_streams(dev, gi_mod, atom):
+    """Two GreenIteration objects (separate plans, separate streams) stepping
+    with no host synchronisation between them share the library's one
+    Gram-Schmidt scratch array; the package orders their turns on it, so each
+    ends bit for bit where it ends when it runs alone -- eagerly and as
+    replayed graphs."""
+    mesh, psi, veff, eps = atom
+    rng = np.random.default_rng(21)
+    psi_b = psi * (1.0 + 0.05 * rng.standard_normal(psi.shape))
+
+    def solo(p0, graph):
+        g, plan = _gi(dev, gi_mod, mesh, p0, veff, eps, "mixed")
+        if graph:
+            g.capture()
+        for _ in range(3):
+            g.step()
+        torch.cuda.synchronize()
+        out = (g.psi.clone(), g.eps.clone())
+        g.close()
+        plan.close()
+        return out
+
+    for graph in (False, True):
+        ref_a, ref_b = solo(psi, graph), solo(psi_b, graph)
+        a, pa = _gi(dev, gi_mod, mesh, psi, veff, eps, "mixed")
+        b, pb = _gi(dev, gi_mod, mesh, psi_b, veff, eps, "mixed")
+        assert a.stream != b.stream
+        if graph:
+            a.capture()
+            b.capture()
+        for _ in range(3):
+            a.step()
+            b.step()
+        torch.cuda.synchronize()
+        assert torch.equal(a.psi, ref_a[0]) and torch.equal(a.eps, ref_a[1]), graph
+        assert torch.equal(b.psi, ref_b[0]) and torch.equal(b.eps, ref_b[1]), graph
+        for o in (a, b):
+            o.close()
+        pa.close()
+        pb.close()
+
+
+def test_capture_runs_an_eager_sweep_first(dev, gi_mod, atom):
+    """capture() on a fresh object runs one eager sweep first (plan scratch,
+    work list and the Gram-Schmidt scratch address all exist before capture),
+    so the replayed sweep equals an eager one."""
+    mesh, psi, veff, eps = atom
+    a, pa = _gi(dev, gi_mod, mesh, psi, veff, eps, "mixed")
+    b, pb = _gi(dev, gi_mod, mesh, psi, veff, eps, "mixed")
+    a.capture()          # one eager sweep happens inside
+    a.replay()
+    b.sweep()
+    b.sweep()
+    torch.cuda.synchronize()
+    assert torch.equal(a.psi, b.psi) and torch.equal(a.eps, b.eps)
+    for o in (a, b):
+        o.close()
+    pa.close()
+    pb.close()

@@ -121,3 +121,55 @@ def test_call_treedriver_dropin(BT, oracle, small_mesh):
                               theta=0.7, degree=7, sourceLeafSize=300, targetLeafSize=300,
                               precision="mixed")
     assert rel_l2(mixed, ref) <= 1e-6
+
+
+def test_exact_symbol_with_the_reference_binding(BT, native, oracle, small_mesh):
+    """A TAGI user points ctypes at this library and binds BaryTreeInterface
+    with the reference's own argtypes tuple (BaryTreeInterface.py:67-72: enum
+    classes for kernel, singularity, approximation and compute type), then
+    calls it the way callTreedriver does (:130-145).  The library default is
+    FP64, so the result equals the oracle's FP64 treecode to 1e-12."""
+    import ctypes
+
+    mesh, f, rho = small_mesh
+    lib = ctypes.CDLL(native.LIB_PATH)
+    dp = ctypes.POINTER(ctypes.c_double)
+    fn = lib.BaryTreeInterface
+    fn.argtypes = (ctypes.c_int, ctypes.c_int, dp, dp, dp, dp, dp, dp, dp, dp, dp, dp, BT.Kernel, ctypes.c_int, dp,
+                   BT.Singularity, BT.Approximation, BT.ComputeType, ctypes.c_double, ctypes.c_int, ctypes.c_int,
+                   ctypes.c_int, ctypes.c_double, ctypes.c_double, ctypes.c_int)
+    arrays = [np.copy(a) for a in (mesh.x, mesh.y, mesh.z, f, mesh.x, mesh.y, mesh.z, f, mesh.w)]
+    kp = np.array([1.0])
+    result = np.zeros(mesh.n)
+    P = lambda a: a.ctypes.data_as(dp)
+    fn(ctypes.c_int(mesh.n), ctypes.c_int(mesh.n), *[P(a) for a in arrays], P(result), BT.Kernel.YUKAWA,
+       ctypes.c_int(1), P(kp), BT.Singularity.SUBTRACTION, BT.Approximation.LAGRANGE,
+       BT.ComputeType.PARTICLE_CLUSTER, ctypes.c_double(0.7), ctypes.c_int(7), ctypes.c_int(300),
+       ctypes.c_int(300), ctypes.c_double(1.0), ctypes.c_double(-1), ctypes.c_int(0))
+    c = oracle.Plan(mesh.x, mesh.y, mesh.z, mesh.x, mesh.y, mesh.z, mesh.w, 0.7, 7, 300, 300, 1.0)
+    ref = c.convolve(f, f, mesh.w, BT.Kernel.YUKAWA, [1.0], BT.Singularity.SUBTRACTION)
+    assert rel_l2(result, ref) <= 1e-12
+    # the enum-typed parameters refuse plain integers, as the reference binding does
+    with pytest.raises(ctypes.ArgumentError):
+        fn(mesh.n, mesh.n, *[P(a) for a in arrays], P(result), 2, 1, P(kp), 2, 1, 1, 0.7, 7, 300, 300, 1.0, -1.0, 0)
+
+
+def test_two_kernel_parameters_k_and_epsilon(BT, small_mesh):
+    """The regularize=True call form (greenIterationFixedPoint.py:223-227,
+    scfFixedPoint.py:246-250) passes Kernel.YUKAWA with
+    numberOfKernelParameters=2 and [k, epsilon].  The YUKAWA and COULOMB
+    kernels read the first parameter only, so that call gives exactly the
+    one-parameter result (the reference itself warns when epsilon != 0)."""
+    mesh, f, rho = small_mesh
+    common = dict(theta=0.7, degree=7, sourceLeafSize=300, targetLeafSize=300)
+
+    def call(nkp, kp):
+        return BT.callTreedriver(mesh.n, mesh.n, np.copy(mesh.x), np.copy(mesh.y), np.copy(mesh.z), np.copy(f),
+                                 np.copy(mesh.x), np.copy(mesh.y), np.copy(mesh.z), np.copy(f), np.copy(mesh.w),
+                                 BT.Kernel.YUKAWA, nkp, kp, BT.Singularity.SUBTRACTION, BT.Approximation.LAGRANGE,
+                                 BT.ComputeType.PARTICLE_CLUSTER, True, 0, **common)
+
+    one = call(1, np.array([1.3]))
+    two = call(2, np.array([1.3, 0.0]))
+    assert np.array_equal(one, two)
+    assert np.array_equal(one, call(2, np.array([1.3, 0.25])))

@@ -35,6 +35,71 @@ def _p(t):
     return ctypes.c_void_p(t.data_ptr())
 
 
+# Largest orbital count whose in-order Gram-Schmidt fits the library's
+# allocation-free scratch (tagi_mgs_dev_noalloc handles targetWavefunction
+# <= 128, i.e. orbitals 0..128).
+NOALLOC_MAX_ORBITALS = 129
+
+# The allocation-free Gram-Schmidt keeps its scratch in ONE fixed device array
+# per GPU, shared by every caller in the process.  Every GreenIteration, SCF
+# and LearnedExtrapolator in this package takes its turn on that array through
+# `mgs_turn`: the stream waits for the last recorded use (an event) before its
+# Gram-Schmidt launches (or a graph replay that holds them) and records its own
+# use after them, so objects stepping on different streams never overlap on
+# the array.  Nothing is waited for or recorded while a stream is being
+# captured; the replay of the captured graph takes its turn instead.
+_MGS_LAST = {}
+
+
+class mgs_turn:
+    """Context manager: order `stream`'s Gram-Schmidt work after every earlier
+    use of the shared scratch in this process, and record this use."""
+
+    def __init__(self, stream):
+        self.stream = stream
+        self.live = False
+
+    def __enter__(self):
+        self.live = not _capturing(self.stream)
+        if self.live:
+            ev = _MGS_LAST.get(self.stream.device)
+            if ev is not None:
+                self.stream.wait_event(ev)
+        return self
+
+    def __exit__(self, et, ev, tb):
+        if self.live and et is None:
+            done = torch.cuda.Event()
+            done.record(self.stream)
+            _MGS_LAST[self.stream.device] = done
+        return False
+
+
+def _capturing(stream):
+    with torch.cuda.stream(stream):
+        return torch.cuda.is_current_stream_capturing()
+
+
+def orthonormalize(psi, weights, stream, first=0):
+    """Weighted Gram-Schmidt of psi's rows first.. in orbital order
+    (Orthogonalization.c:14-119 per row) on `stream`.  Up to 129 orbitals the
+    allocation-free entry point runs, in the package-wide turn on its shared
+    scratch; above that the allocating tagi_mgs_dev does (not capturable)."""
+    L = _native.lib()
+    m, n = int(psi.shape[0]), int(psi.shape[1])
+    s = ctypes.c_void_p(stream.cuda_stream)
+    if m <= NOALLOC_MAX_ORBITALS:
+        with mgs_turn(stream):
+            for j in range(first, m):
+                _native.check(L.tagi_mgs_dev_noalloc(_p(psi), _p(psi[j]), _p(weights), j, n, m, s))
+    else:
+        if _capturing(stream):
+            raise RuntimeError(f"{m} orbitals: Gram-Schmidt above {NOALLOC_MAX_ORBITALS} orbitals allocates and "
+                               "cannot be captured")
+        for j in range(first, m):
+            _native.check(L.tagi_mgs_dev(_p(psi), _p(psi[j]), _p(weights), j, n, m, s))
+
+
 class GreenIteration:
     """Device state and launch sequence of simultaneous Green iteration.
 
@@ -73,6 +138,7 @@ class GreenIteration:
         nw = int(L.tagi_gi_workspace_doubles(self.n, self.norb))
         self.work = torch.empty(nw, **f64)
         self._graph = None
+        self._eager_sweeps = 0
         self.anderson = None
 
     def set_eigenvalues(self, eps):
@@ -91,9 +157,7 @@ class GreenIteration:
                                        1.0 / (4.0 * math.pi), _p(self.eps), _p(self.eps_prev), _p(self.k),
                                        self.gauge, _p(self.dE), _p(self.flags), _p(self.work),
                                        self.work.numel(), s))
-        for j in range(m):
-            row = self.psi[j]
-            _native.check(L.tagi_mgs_dev_noalloc(_p(self.psi), _p(row), _p(self.w), j, n, m, s))
+        orthonormalize(self.psi, self.w, self.stream)
         _native.check(L.tagi_gi_residual(_p(self.psi), _p(self.psi_prev), _p(self.w), n, m, _p(self.eps),
                                          _p(self.eps_prev), _p(self.res), _p(self.psi_res), _p(self.work),
                                          self.work.numel(), s))
@@ -102,9 +166,19 @@ class GreenIteration:
         """One sweep, launched eagerly on the stream."""
         with torch.cuda.stream(self.stream):
             self._launches()
+        self._eager_sweeps += 1
 
     def capture(self):
-        """Record one sweep as a CUDA graph (after at least one eager sweep)."""
+        """Record one sweep as a CUDA graph.  A captured sweep must not allocate
+        or look anything up: the plan's scratch and work list, and the
+        Gram-Schmidt scratch address, come from an earlier eager sweep, so one
+        runs here first if none has.  Above 129 orbitals the sweep's
+        Gram-Schmidt allocates and capture is refused."""
+        if self.norb > NOALLOC_MAX_ORBITALS:
+            raise RuntimeError(f"{self.norb} orbitals: sweeps above {NOALLOC_MAX_ORBITALS} orbitals are not "
+                               "capturable (their Gram-Schmidt allocates); use sweep()")
+        if self._eager_sweeps == 0:
+            self.sweep()
         if self._graph is not None:
             self._graph.close()
         with torch.cuda.stream(self.stream):
@@ -116,7 +190,8 @@ class GreenIteration:
     def replay(self):
         if self._graph is None:
             raise RuntimeError("capture() first")
-        self._graph.replay(self.stream)
+        with mgs_turn(self.stream):   # the graph holds Gram-Schmidt launches
+            self._graph.replay(self.stream)
 
     def step(self):
         """One sweep: graph replay when captured, else eager."""
@@ -194,8 +269,7 @@ class GreenIteration:
             c_t = torch.as_tensor(c, dtype=torch.float64, device=self.psi.device).contiguous()
             _native.check(L.tagi_gi_anderson_mix(_p(a["X"]), _p(a["F"]), nh, row, _p(rows_t), _p(c_t), a["beta"], m,
                                                  n, _p(self.psi), s))
-            for j in range(m):  # the mixed orbitals are no longer orthonormal
-                _native.check(L.tagi_mgs_dev_noalloc(_p(self.psi), _p(self.psi[j]), _p(self.w), j, n, m, s))
+            orthonormalize(self.psi, self.w, self.stream)  # the mixed orbitals are no longer orthonormal
             self.set_eigenvalues(eps_new)
             self.stream.synchronize()
         a["mixed"] += 1

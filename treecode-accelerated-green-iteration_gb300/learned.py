@@ -22,8 +22,10 @@ import torch
 
 try:
     from . import _native
+    from .gi import orthonormalize
 except ImportError:
     import _native
+    from gi import orthonormalize
 
 
 def _p(t):
@@ -246,8 +248,7 @@ class LearnedExtrapolator:
                                                  _p(self.net.params["alpha"]), gi.norb, self.ncell, self.P, gi.n,
                                                  _p(self.work_psi), _p(self.work_d), s))
         gi.psi.copy_(self.work_psi)
-        for j in range(gi.norb):
-            _native.check(L.tagi_mgs_dev_noalloc(_p(gi.psi), _p(gi.psi[j]), _p(gi.w), j, gi.n, gi.norb, s))
+        orthonormalize(gi.psi, gi.w, gi.stream)
         self.work_psi.copy_(gi.psi)  # the proposal as the next sweep starts from it
         gi.set_eigenvalues(self.eps_proposed)
         self.pending = True

@@ -35,12 +35,12 @@ try:
     from . import _native
     from . import device as dev
     from .BaryTreeInterface import Kernel, Singularity
-    from .gi import GreenIteration
+    from .gi import GreenIteration, orthonormalize
 except ImportError:
     import _native
     import device as dev
     from BaryTreeInterface import Kernel, Singularity
-    from gi import GreenIteration
+    from gi import GreenIteration, orthonormalize
 
 KB = 1.0 / 315774.6  # Ha per K (scfFixedPoint.py:48-50)
 
@@ -181,9 +181,7 @@ class SCF:
                                 device="cuda")
         self.dot = torch.zeros(4, dtype=torch.float64, device="cuda")
         # orthonormal start
-        for j in range(self.norb):
-            _native.check(L.tagi_mgs_dev_noalloc(_p(self.psi), _p(self.psi[j]), _p(self.w), j, self.n,
-                                                 self.norb, self.s))
+        orthonormalize(self.psi, self.w, self.stream)
         self.gi = GreenIteration(self.plan, self.w, self.psi, eps0, self.veff, gauge_shift=self.gauge,
                                  precision=self.precision, stream=self.stream)
         self.mixer = AndersonMixer(self.n, self.w, mixing, history, stream=self.stream)

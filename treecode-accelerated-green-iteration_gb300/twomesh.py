@@ -77,6 +77,7 @@ class TwoMeshCorrection:
                  gauge_shift=-0.5, gaussian_alpha=1.0, soft=0.0, stream=None):
         self.stream = stream if stream is not None else torch.cuda.current_stream()
         self.s = ctypes.c_void_p(self.stream.cuda_stream)
+        self.stream.wait_stream(torch.cuda.current_stream())  # mesh arrays made on the caller's stream
         with torch.cuda.stream(self.stream):
             self.X, self.Y, self.Z, self.W = (_t(a) for a in (X, Y, Z, W))
             self.Xf, self.Yf, self.Zf, self.Wf = (_t(a) for a in (Xf, Yf, Zf, Wf))
@@ -112,6 +113,7 @@ class TwoMeshCorrection:
             rho_f = self.interpolate(rho)
             vh = self.plan.convolve(rho, rho_f, Kernel.COULOMB, [self.alpha], Singularity.SUBTRACTION,
                                     precision=self.precision, stream=self.stream)
+        torch.cuda.current_stream().wait_stream(self.stream)  # results ready for the caller's stream
         return vh, rho_f
 
     def correct(self, psi, eps, rho, n_electrons=None, sigma=None):
