@@ -418,13 +418,22 @@ int tagi_beta_parameters(double beta, double *theta, int *degree, int *sourceLea
  * waits for the recorded events, returns summed milliseconds and mark
  * counts per phase (nphase >= 7), and clears the record. */
 long long tagi_launch_count(void);
-/* Pair-throughput ceiling of the mixed-precision field kernels on this GPU:
- * their inner-loop arithmetic (variant 0: near-field loop, 1: far-field
- * proxy-grid loop, 2: Yukawa orbital-group near loop, 8 orbitals per pair,
- * counted per pair and orbital) with operands in shared memory and registers
- * and no global-memory traffic, timed with CUDA events.  Pair interactions / s. */
+/* Pair-throughput ceiling of the mixed-precision field kernels' inner loops
+ * on this GPU: their arithmetic (variant 0: near-field loop, 1: far-field
+ * proxy-grid loop, 2: Yukawa orbital-group near loop and 3: Yukawa
+ * orbital-group far loop, 8 orbitals per pair geometry, counted per pair and
+ * orbital) with operands in shared memory and registers and no global-memory
+ * traffic, timed with CUDA events.  Pair interactions / s.  A field kernel's
+ * rate over this is its loop efficiency, not a hardware roofline. */
 int tagi_pair_peak(int kernel, int singularity, int variant, double kernelParameter,
                    double *pairsPerSecond, void *stream);
+/* Hardware pipe rates of this GPU, measured with every SM busy and no memory
+ * traffic, in lane operations per second: rates[0] FP32 FFMA, rates[1]
+ * packed FFMA2 (two lanes per instruction), rates[2] MUFU ex2, rates[3]
+ * MUFU rsqrt, rates[4] the SM clock in MHz seen during the FFMA run (clock64
+ * cycles over CUDA-event time), rates[5] the number of SMs.  The field
+ * kernels' roofline is their arithmetic per pair against these rates. */
+int tagi_pipe_rates(double *rates, void *stream);
 int tagi_profile(int enable);
 int tagi_profile_read(double *ms, long long *count, int nphase);
 

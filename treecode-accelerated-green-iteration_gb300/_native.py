@@ -94,6 +94,7 @@ SIGNATURES = {
     "tagi_beta_parameters": (_i, [_d, _dp, _ip, _ip, _ip]),
     "tagi_launch_count": (ctypes.c_longlong, []),
     "tagi_pair_peak": (_i, [_i, _i, _i, _d, _dp, _vp]),
+    "tagi_pipe_rates": (_i, [_dp, _vp]),
     "tagi_profile": (_i, [_i]),
     "tagi_profile_read": (_i, [_dp, ctypes.POINTER(ctypes.c_longlong), _i]),
     "tagi_last_error": (_i, []),

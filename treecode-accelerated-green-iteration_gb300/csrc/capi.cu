@@ -494,8 +494,9 @@ int tagi_pair_peak(int kernel, int singularity, int variant, double kernelParame
                    void *stream) {
     if (!pairsPerSecond) return set_error(TAGI_ERR_ARG, "null output");
     if (kernel != KERNEL_COULOMB && kernel != KERNEL_YUKAWA) return set_error(TAGI_ERR_UNSUPPORTED, "kernel %d", kernel);
-    if (variant < 0 || variant > 2)
-        return set_error(TAGI_ERR_ARG, "variant must be 0 (near), 1 (far) or 2 (near, orbital groups)");
+    if (variant < 0 || variant > 3)
+        return set_error(TAGI_ERR_ARG,
+                         "variant must be 0 (near), 1 (far), 2 (near, orbital groups) or 3 (far, orbital groups)");
     return pair_peak(kernel, singularity, variant, kernelParameter, pairsPerSecond, (cudaStream_t)stream);
 }
 

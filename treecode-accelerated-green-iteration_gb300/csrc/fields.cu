@@ -104,27 +104,43 @@ __device__ __forceinline__ int next_item(int *queue, int *s_item) {
     return *s_item;
 }
 
-// One pair from its squared scaled distance r2 = r'^2; MASK drops the
-// coincident (r = 0) pair.
-template <int KERN, bool SS, bool MASK>
-__device__ __forceinline__ float pair_r2(float r2, float q, float w, float fi, float acc) {
-    float rinv = rsqrt_mufu(r2);
-    if (MASK) rinv = r2 > 0.f ? rinv : 0.f;
-    if (KERN == KERNEL_YUKAWA) {
-        const float g = ex2_mufu(-(r2 * rinv)) * rinv;
-        return fmaf(g, SS ? fmaf(-fi, w, q) : q, acc);
-    } else if (SS) {
-        const float e = ex2_mufu(-r2);
-        return fmaf(rinv, fmaf(-fi * e, w, q), acc);
-    } else {
-        return fmaf(rinv, q, acc);
-    }
-}
+// Packed FP32 pairs.  On the sm_100 family one FADD2 / FMUL2 / FFMA2
+// instruction applies the same round-to-nearest IEEE operation to two lanes
+// held in a register pair, so the pair arithmetic takes half the issue slots
+// of its scalar form with bit-identical per-lane results.  The field kernels
+// pack two SOURCES (near field) or two proxy points (far field) per
+// operation; a target's own values are duplicated once into both lanes.
+__device__ __forceinline__ float2 dup2(float a) { return make_float2(a, a); }
+__device__ __forceinline__ float2 add2(float2 a, float2 b) { return __fadd2_rn(a, b); }
+__device__ __forceinline__ float2 mul2(float2 a, float2 b) { return __fmul2_rn(a, b); }
+__device__ __forceinline__ float2 fma2(float2 a, float2 b, float2 c) { return __ffma2_rn(a, b, c); }
+__device__ __forceinline__ float2 rsqrt2(float2 a) { return make_float2(rsqrt_mufu(a.x), rsqrt_mufu(a.y)); }
+// 2^{-a} per lane
+__device__ __forceinline__ float2 ex2neg2(float2 a) { return make_float2(ex2_mufu(-a.x), ex2_mufu(-a.y)); }
+// 2^{a} per lane
+__device__ __forceinline__ float2 ex2pos2(float2 a) { return make_float2(ex2_mufu(a.x), ex2_mufu(a.y)); }
 
+// Two pairs (one target, two sources) from their squared scaled distances
+// r2 = r'^2; q, w the two sources' charges and weights, nfi = -f_i in both
+// lanes.  Per lane:
+//   Yukawa   acc += 2^{-r'} / r' * (SS ? q - f_i w : q)
+//   Coulomb  acc += (SS ? q - f_i 2^{-r'^2} w : q) / r'
+// MASK zeroes a coincident (r = 0) pair.
 template <int KERN, bool SS, bool MASK>
-__device__ __forceinline__ float pair_scaled(float dx, float dy, float dz, float q, float w, float fi,
-                                             float acc) {
-    return pair_r2<KERN, SS, MASK>(fmaf(dx, dx, fmaf(dy, dy, dz * dz)), q, w, fi, acc);
+__device__ __forceinline__ float2 pair2(float2 r2, float2 q, float2 w, float2 nfi, float2 acc) {
+    float2 rinv = rsqrt2(r2);
+    if (MASK) {
+        rinv.x = r2.x > 0.f ? rinv.x : 0.f;
+        rinv.y = r2.y > 0.f ? rinv.y : 0.f;
+    }
+    if (KERN == KERNEL_YUKAWA) {
+        const float2 g = mul2(ex2neg2(mul2(r2, rinv)), rinv);
+        return fma2(g, SS ? fma2(nfi, w, q) : q, acc);
+    } else if (SS) {
+        return fma2(rinv, fma2(mul2(nfi, ex2neg2(r2)), w, q), acc);
+    } else {
+        return fma2(rinv, q, acc);
+    }
 }
 
 // Compensated (Kahan) addition of an FP32 partial into (sum, cmp).
@@ -135,75 +151,76 @@ __device__ __forceinline__ void kahan_add(float &sum, float &cmp, float part) {
     sum = t;
 }
 
-// One staged tile against NT targets.  Pairs are summed in FP32 in chunks of
-// KCHUNK and each chunk is added to the target's Kahan sum: a long FP32 run
-// loses ~sqrt(n) u of its total, and singularity subtraction multiplies that
-// loss by |f_i int G| / |phi_i| (often 10-100).
-// Ordinary tiles: s_a[j] = (scaled batch-relative x, y, z, q), s_b[j].w = w.
-// PRECISE tiles (close ranges): s_a[j] = (x_hi, y_hi, z_hi, q) and
-// s_b[j] = (x_lo, y_lo, z_lo, w) are FP32 splits of the absolute FP64
-// coordinates, the targets likewise; each difference is (t_hi - s_hi) +
-// (t_lo - s_lo) -- exact hi differences for nearby points -- and the unscaled
-// r^2 is multiplied by sc2 = sc^2, so the shortest pairs keep FP32 relative
-// precision in r whatever the batch size.
+__device__ __forceinline__ float4 lds4(const float *p) { return *reinterpret_cast<const float4 *>(p); }
+__device__ __forceinline__ float2 lds2(const float *p) { return *reinterpret_cast<const float2 *>(p); }
+
+// Near-field source tile in shared memory, structure of arrays, NEGATED
+// coordinates so that one FADD2 forms t - s for two sources:
+//   row 0..2  -x, -y, -z   (ordinary tiles: scaled batch-relative FP32;
+//                           PRECISE tiles: hi parts of the absolute FP64
+//                           coordinates' FP32 splits)
+//   row 3, 4  charge q = f w, weight w
+//   row 5..7  -lo parts of the splits (PRECISE tiles only)
+// A tile of cnt sources is padded to cnt4 = a multiple of 4 with copies of
+// its first source carrying q = w = 0: their terms are exactly +-0.
+//
+// One tile against NT targets, two sources per packed operation.  Pairs are
+// summed in FP32 per lane over chunks of KCHUNK sources; each chunk's two
+// lane sums are added and the result enters the target's Kahan sum: a long
+// FP32 run loses ~sqrt(n) u of its total, and singularity subtraction
+// multiplies that loss by |f_i int G| / |phi_i| (often 10-100).
+// PRECISE tiles (close ranges): each difference is (t_hi - s_hi) +
+// (t_lo - s_lo) -- exact hi differences for nearby points -- and the
+// unscaled r^2 is multiplied by sc2 = sc^2, so the shortest pairs keep FP32
+// relative precision in r whatever the batch size.
 constexpr int KCHUNK = 64;
+constexpr int NROWS_PRECISE = 8;
 template <int KERN, bool SS, bool MASK, bool PRECISE, int NT>
-__device__ __forceinline__ void near_tile(const float4 *__restrict__ s_a, const float4 *__restrict__ s_b,
-                                          int cnt, const float (&tx)[NT], const float (&ty)[NT],
-                                          const float (&tz)[NT], const float *__restrict__ s_tl, float sc2,
-                                          const float (&fi)[NT], float (&sum)[NT], float (&cmp)[NT]) {
-    // lo parts of this thread's targets (only live inside PRECISE tiles)
-    float lx[NT], ly[NT], lz[NT];
+__device__ __forceinline__ void near_tile(const float (*__restrict__ s)[NTILE], int cnt4, const float2 (&tx)[NT],
+                                          const float2 (&ty)[NT], const float2 (&tz)[NT], const float2 (&lx)[NT],
+                                          const float2 (&ly)[NT], const float2 (&lz)[NT], float2 sc2,
+                                          const float2 (&nfi)[NT], float (&sum)[NT], float (&cmp)[NT]) {
+    for (int j0 = 0; j0 < cnt4; j0 += KCHUNK) {
+        const int j1 = min(j0 + KCHUNK, cnt4);
+        float2 part[NT];
 #pragma unroll
-    for (int k = 0; k < NT; k++) {
-        lx[k] = PRECISE ? s_tl[3 * k] : 0.f;
-        ly[k] = PRECISE ? s_tl[3 * k + 1] : 0.f;
-        lz[k] = PRECISE ? s_tl[3 * k + 2] : 0.f;
-    }
-    for (int j0 = 0; j0 < cnt; j0 += KCHUNK) {
-        const int j1 = min(j0 + KCHUNK, cnt);
-        float part[NT];
-#pragma unroll
-        for (int k = 0; k < NT; k++) part[k] = 0.f;
-        if (j1 - j0 == KCHUNK) {
-#pragma unroll 8
-            for (int j = j0; j < j0 + KCHUNK; j++) {
-                const float4 sa = s_a[j];
-                if (PRECISE) {
-                    const float4 sb = s_b[j];
-#pragma unroll
-                    for (int k = 0; k < NT; k++) {
-                        const float dx = (tx[k] - sa.x) + (lx[k] - sb.x);
-                        const float dy = (ty[k] - sa.y) + (ly[k] - sb.y);
-                        const float dz = (tz[k] - sa.z) + (lz[k] - sb.z);
-                        part[k] = pair_r2<KERN, SS, MASK>(fmaf(dx, dx, fmaf(dy, dy, dz * dz)) * sc2, sa.w, sb.w,
-                                                          fi[k], part[k]);
-                    }
-                } else {
-                    const float w = s_b[j].w;
-#pragma unroll
-                    for (int k = 0; k < NT; k++)
-                        part[k] = pair_scaled<KERN, SS, MASK>(tx[k] - sa.x, ty[k] - sa.y, tz[k] - sa.z, sa.w, w,
-                                                              fi[k], part[k]);
-                }
-            }
-        } else {
+        for (int k = 0; k < NT; k++) part[k] = make_float2(0.f, 0.f);
 #pragma unroll 2
-            for (int j = j0; j < j1; j++) {
-                const float4 sa = s_a[j];
-                const float4 sb = s_b[j];
+        for (int j = j0; j < j1; j += 4) {
+            const float4 X = lds4(s[0] + j), Y = lds4(s[1] + j), Z = lds4(s[2] + j);
+            const float4 Q = lds4(s[3] + j), W = lds4(s[4] + j);
+            float4 XL = make_float4(0.f, 0.f, 0.f, 0.f), YL = XL, ZL = XL;
+            if constexpr (PRECISE) {
+                XL = lds4(s[5] + j);
+                YL = lds4(s[6] + j);
+                ZL = lds4(s[7] + j);
+            }
+#pragma unroll
+            for (int h = 0; h < 2; h++) {
+                const float2 sx = h ? make_float2(X.z, X.w) : make_float2(X.x, X.y);
+                const float2 sy = h ? make_float2(Y.z, Y.w) : make_float2(Y.x, Y.y);
+                const float2 sz = h ? make_float2(Z.z, Z.w) : make_float2(Z.x, Z.y);
+                const float2 q = h ? make_float2(Q.z, Q.w) : make_float2(Q.x, Q.y);
+                const float2 w = h ? make_float2(W.z, W.w) : make_float2(W.x, W.y);
+                const float2 sxl = h ? make_float2(XL.z, XL.w) : make_float2(XL.x, XL.y);
+                const float2 syl = h ? make_float2(YL.z, YL.w) : make_float2(YL.x, YL.y);
+                const float2 szl = h ? make_float2(ZL.z, ZL.w) : make_float2(ZL.x, ZL.y);
 #pragma unroll
                 for (int k = 0; k < NT; k++) {
-                    const float dx = PRECISE ? (tx[k] - sa.x) + (lx[k] - sb.x) : tx[k] - sa.x;
-                    const float dy = PRECISE ? (ty[k] - sa.y) + (ly[k] - sb.y) : ty[k] - sa.y;
-                    const float dz = PRECISE ? (tz[k] - sa.z) + (lz[k] - sb.z) : tz[k] - sa.z;
-                    const float r2 = fmaf(dx, dx, fmaf(dy, dy, dz * dz));
-                    part[k] = pair_r2<KERN, SS, MASK>(PRECISE ? r2 * sc2 : r2, sa.w, sb.w, fi[k], part[k]);
+                    float2 dx = add2(tx[k], sx), dy = add2(ty[k], sy), dz = add2(tz[k], sz);
+                    if (PRECISE) {
+                        dx = add2(dx, add2(lx[k], sxl));
+                        dy = add2(dy, add2(ly[k], syl));
+                        dz = add2(dz, add2(lz[k], szl));
+                    }
+                    float2 r2 = fma2(dx, dx, fma2(dy, dy, mul2(dz, dz)));
+                    if (PRECISE) r2 = mul2(r2, sc2);
+                    part[k] = pair2<KERN, SS, MASK>(r2, q, w, nfi[k], part[k]);
                 }
             }
         }
 #pragma unroll
-        for (int k = 0; k < NT; k++) kahan_add(sum[k], cmp[k], part[k]);
+        for (int k = 0; k < NT; k++) kahan_add(sum[k], cmp[k], part[k].x + part[k].y);
     }
 }
 
@@ -218,18 +235,16 @@ __device__ __forceinline__ void split_f32(double v, float &hi, float &lo) {
 // ---------------------------------------------------------------------------
 // PASS 0 handles the ordinary near ranges, PASS 1 the close ones (double-float
 // coordinates, r = 0 mask) into a second output; two passes keep each
-// kernel's register footprint at two tile variants.
+// kernel's register footprint at one tile variant's.
 #ifndef TAGI_NEAR_MINB
 #define TAGI_NEAR_MINB 3   // resident CTAs per SM the near kernel is compiled for
 #endif
 template <int KERN, bool SS, int NT, int PASS>
 __global__ void __launch_bounds__(FT, TAGI_NEAR_MINB) near_mixed(const __grid_constant__ Work w) {
-    __shared__ float4 s_a[NTILE];
-    __shared__ float4 s_b[NTILE];
-    __shared__ float s_tlo[FT * NT * 3];
+    constexpr int NR = PASS == 1 ? NROWS_PRECISE : 5;
+    __shared__ __align__(16) float s_src[NR][NTILE];
     __shared__ int s_item;
     const int tid = threadIdx.x;
-    float *my_tl = s_tlo + 3 * NT * tid;
     for (;;) {
         const int item = next_item(w.queue, &s_item);
         if (item >= w.nitems) break;
@@ -242,7 +257,7 @@ __global__ void __launch_bounds__(FT, TAGI_NEAR_MINB) near_mixed(const __grid_co
                      cbz = a.tcenter[3L * bn + 2];
         const float scf = a.kc32[orb];
         const double sc = (double)scf;
-        const float sc2 = (float)(sc * sc);
+        const float2 sc2 = dup2((float)(sc * sc));
         const float *q = a.q32 + (long)orb * a.ns;
         const float *ft = a.ft32 + (long)orb * a.nt;
         const int r0 = a.rng_off[b], r1 = a.rng_off[b + 1];
@@ -250,26 +265,28 @@ __global__ void __launch_bounds__(FT, TAGI_NEAR_MINB) near_mixed(const __grid_co
             // consecutive targets per thread: the threads with targets form a
             // prefix, so whole warps past it have none and skip the pair loops
             const bool warp_busy = base + NT * (tid & ~31) < te;
-            float tx[NT], ty[NT], tz[NT], fi[NT], sum[NT], cmp[NT];
+            float2 tx[NT], ty[NT], tz[NT], lx[NT], ly[NT], lz[NT], nfi[NT];
+            float sum[NT], cmp[NT];
 #pragma unroll
             for (int k = 0; k < NT; k++) {
-                int i = base + NT * tid + k;
-                bool v = i < te;
+                const int i = base + NT * tid + k;
+                const bool v = i < te;
                 if (PASS == 1) {
                     const float4 h = v ? a.thi[i] : make_float4(0.f, 0.f, 0.f, 0.f);
                     const float4 l = v ? a.tlo[i] : make_float4(0.f, 0.f, 0.f, 0.f);
-                    tx[k] = h.x;
-                    ty[k] = h.y;
-                    tz[k] = h.z;
-                    my_tl[3 * k] = l.x;
-                    my_tl[3 * k + 1] = l.y;
-                    my_tl[3 * k + 2] = l.z;
+                    tx[k] = dup2(h.x);
+                    ty[k] = dup2(h.y);
+                    tz[k] = dup2(h.z);
+                    lx[k] = dup2(l.x);
+                    ly[k] = dup2(l.y);
+                    lz[k] = dup2(l.z);
                 } else {
-                    tx[k] = v ? (float)((a.tx[i] - cbx) * sc) : 0.f;
-                    ty[k] = v ? (float)((a.ty[i] - cby) * sc) : 0.f;
-                    tz[k] = v ? (float)((a.tz[i] - cbz) * sc) : 0.f;
+                    tx[k] = dup2(v ? (float)((a.tx[i] - cbx) * sc) : 0.f);
+                    ty[k] = dup2(v ? (float)((a.ty[i] - cby) * sc) : 0.f);
+                    tz[k] = dup2(v ? (float)((a.tz[i] - cbz) * sc) : 0.f);
+                    lx[k] = ly[k] = lz[k] = dup2(0.f);
                 }
-                fi[k] = v ? ft[i] : 0.f;
+                nfi[k] = dup2(v ? -ft[i] : 0.f);
                 sum[k] = 0.f;
                 cmp[k] = 0.f;
             }
@@ -286,38 +303,42 @@ __global__ void __launch_bounds__(FT, TAGI_NEAR_MINB) near_mixed(const __grid_co
                 const bool noexp = KERN == KERNEL_COULOMB && SS && dm * dm > 40.f;
                 for (int t0 = rb; t0 < r.y; t0 += NTILE) {
                     const int cnt = min(NTILE, r.y - t0);
+                    const int cnt4 = (cnt + 3) & ~3;
                     __syncthreads();
-                    for (int j = tid; j < cnt; j += FT) {
-                        const int jj = t0 + j;
-                        float4 sa, sb;
-                        if (PASS == 1) {
-                            sa = a.shi[jj];
-                            sb = a.slo[jj];
+                    for (int j = tid; j < cnt4; j += FT) {
+                        const bool real = j < cnt;
+                        const int jj = t0 + (real ? j : 0);   // padding: a copy of the first source
+                        if constexpr (PASS == 1) {
+                            const float4 h = a.shi[jj], l = a.slo[jj];
+                            s_src[0][j] = -h.x;
+                            s_src[1][j] = -h.y;
+                            s_src[2][j] = -h.z;
+                            s_src[5][j] = -l.x;
+                            s_src[6][j] = -l.y;
+                            s_src[7][j] = -l.z;
                         } else {
-                            sa.x = (float)((a.sx[jj] - cbx) * sc);
-                            sa.y = (float)((a.sy[jj] - cby) * sc);
-                            sa.z = (float)((a.sz[jj] - cbz) * sc);
-                            sb.x = sb.y = sb.z = 0.f;
+                            s_src[0][j] = -(float)((a.sx[jj] - cbx) * sc);
+                            s_src[1][j] = -(float)((a.sy[jj] - cby) * sc);
+                            s_src[2][j] = -(float)((a.sz[jj] - cbz) * sc);
                         }
-                        sa.w = q[jj];
-                        sb.w = a.w32[jj];
-                        s_a[j] = sa;
-                        s_b[j] = sb;
+                        s_src[3][j] = real ? q[jj] : 0.f;
+                        s_src[4][j] = real ? a.w32[jj] : 0.f;
                     }
                     __syncthreads();
                     if (!warp_busy) continue;
                     if (PASS == 1)
-                        near_tile<KERN, SS, true, true, NT>(s_a, s_b, cnt, tx, ty, tz, my_tl, sc2, fi, sum, cmp);
+                        near_tile<KERN, SS, true, true, NT>(s_src, cnt4, tx, ty, tz, lx, ly, lz, sc2, nfi, sum, cmp);
                     else if (noexp)
-                        near_tile<KERN, false, false, false, NT>(s_a, s_b, cnt, tx, ty, tz, my_tl, sc2, fi, sum,
+                        near_tile<KERN, false, false, false, NT>(s_src, cnt4, tx, ty, tz, lx, ly, lz, sc2, nfi, sum,
                                                                  cmp);
                     else
-                        near_tile<KERN, SS, false, false, NT>(s_a, s_b, cnt, tx, ty, tz, my_tl, sc2, fi, sum, cmp);
+                        near_tile<KERN, SS, false, false, NT>(s_src, cnt4, tx, ty, tz, lx, ly, lz, sc2, nfi, sum,
+                                                              cmp);
                 }
             }
 #pragma unroll
             for (int k = 0; k < NT; k++) {
-                int i = base + NT * tid + k;
+                const int i = base + NT * tid + k;
                 if (i < te) a.out[(long)orb * a.nt + i] = ((double)sum[k] - (double)cmp[k]) * sc;
             }
         }
@@ -326,75 +347,74 @@ __global__ void __launch_bounds__(FT, TAGI_NEAR_MINB) near_mixed(const __grid_co
 
 // ---------------------------------------------------------------------------
 // Far field, mixed precision.  The proxy grid is a tensor product, so r'^2
-// is assembled from per-axis squares (one add per pair).  Two targets per
-// thread share every shared-memory read.  Coulomb subtraction: when the
-// whole cluster lies so far that r'^2 > 40 for every proxy point, the
-// Gaussian term f_i what_k 2^{-r'^2} is below 2^-40 of f_i what_k and is
-// dropped (one MUFU op less per pair); Yukawa clusters with r' > 127
-// everywhere add exactly 0 in FP32 (2^{-r'} flushes to zero) and are skipped.
+// is assembled from per-axis squares: one packed add per two proxy points.
+// Two proxy points along the innermost axis share each packed operation; the
+// staged charges and weights have that axis padded to an even length n1p
+// (padding: charge and weight 0, the distance of the first point).  Coulomb
+// subtraction: when the whole cluster lies so far that r'^2 > 40 for every
+// proxy point, the Gaussian term f_i what_k 2^{-r'^2} is below 2^-40 of
+// f_i what_k and is dropped (one MUFU op less per pair); Yukawa clusters
+// with r' > 127 everywhere add exactly 0 in FP32 (2^{-r'} flushes to zero)
+// and are skipped.
 // ---------------------------------------------------------------------------
+template <int MAXN1>
+__host__ __device__ constexpr int even_up() { return MAXN1 + (MAXN1 & 1); }
+
 template <int KERN, bool SS, bool EXPTERM, int MAXN1, int NT>
-__device__ __forceinline__ void far_cluster(const float2 *__restrict__ s_qw, const float (*s_p)[MAXN1],
-                                            int n1, const float (&tx)[NT], const float (&ty)[NT],
-                                            const float (&tz)[NT], const float (&fi)[NT],
-                                            float (&sum)[NT], float (&cmp)[NT]) {
-    float dz2[NT][MAXN1];
+__device__ __forceinline__ void far_cluster(const float *__restrict__ s_q, const float *__restrict__ s_w,
+                                            const float (*s_p)[MAXN1], int n1, const float (&tx)[NT],
+                                            const float (&ty)[NT], const float (&tz)[NT],
+                                            const float2 (&nfi)[NT], float (&sum)[NT], float (&cmp)[NT]) {
+    constexpr int MH = even_up<MAXN1>() / 2;
+    constexpr bool PSS = KERN == KERNEL_YUKAWA ? SS : (SS && EXPTERM);
+    const int n1p = n1 + (n1 & 1);
+    float2 dz2[NT][MH];
 #pragma unroll
     for (int k = 0; k < NT; k++)
 #pragma unroll
-        for (int m = 0; m < MAXN1; m++) {
-            float d = tz[k] - s_p[2][m < n1 ? m : 0];
-            dz2[k][m] = d * d;
+        for (int m = 0; m < MH; m++) {
+            const float d0 = tz[k] - s_p[2][2 * m < n1 ? 2 * m : 0];
+            const float d1 = tz[k] - s_p[2][2 * m + 1 < n1 ? 2 * m + 1 : 0];
+            dz2[k][m] = make_float2(d0 * d0, d1 * d1);
         }
     int idx = 0;
     for (int k1 = 0; k1 < n1; k1++) {  // one (n+1)^2 slab per FP32 partial, then Kahan
-        float part[NT];
-#pragma unroll
-        for (int k = 0; k < NT; k++) part[k] = 0.f;
+        float2 part[NT];
         float dx2[NT];
 #pragma unroll
         for (int k = 0; k < NT; k++) {
+            part[k] = make_float2(0.f, 0.f);
             const float dx = tx[k] - s_p[0][k1];
             dx2[k] = dx * dx;
         }
         for (int k2 = 0; k2 < n1; k2++) {
-            float rxy[NT];
+            float2 rxy[NT];
 #pragma unroll
             for (int k = 0; k < NT; k++) {
                 const float dy = ty[k] - s_p[1][k2];
-                rxy[k] = fmaf(dy, dy, dx2[k]);
+                rxy[k] = dup2(fmaf(dy, dy, dx2[k]));
             }
 #pragma unroll
-            for (int k3 = 0; k3 < MAXN1; k3++) {
-                if (k3 < n1) {
-                    const float2 qw = s_qw[idx + k3];
+            for (int m = 0; m < MH; m++) {
+                if (2 * m < n1) {
+                    const float2 q = lds2(s_q + idx + 2 * m), wv = lds2(s_w + idx + 2 * m);
 #pragma unroll
-                    for (int k = 0; k < NT; k++) {
-                        const float r2 = rxy[k] + dz2[k][k3];
-                        const float rinv = rsqrt_mufu(r2);
-                        if (KERN == KERNEL_YUKAWA) {
-                            const float g = ex2_mufu(-(r2 * rinv)) * rinv;
-                            part[k] = fmaf(g, SS ? fmaf(-fi[k], qw.y, qw.x) : qw.x, part[k]);
-                        } else if (SS && EXPTERM) {
-                            const float ex = ex2_mufu(-r2);
-                            part[k] = fmaf(rinv, fmaf(-fi[k] * ex, qw.y, qw.x), part[k]);
-                        } else {
-                            part[k] = fmaf(rinv, qw.x, part[k]);
-                        }
-                    }
+                    for (int k = 0; k < NT; k++)
+                        part[k] = pair2<KERN, PSS, false>(add2(rxy[k], dz2[k][m]), q, wv, nfi[k], part[k]);
                 }
             }
-            idx += n1;
+            idx += n1p;
         }
 #pragma unroll
-        for (int k = 0; k < NT; k++) kahan_add(sum[k], cmp[k], part[k]);
+        for (int k = 0; k < NT; k++) kahan_add(sum[k], cmp[k], part[k].x + part[k].y);
     }
 }
 
 template <int KERN, bool SS, int MAXN1, int NT>
 __global__ void __launch_bounds__(FT, 2) far_mixed(const __grid_constant__ Work w) {
-    constexpr int MAXP = MAXN1 * MAXN1 * MAXN1;
-    __shared__ float2 s_qw[MAXP];
+    constexpr int MAXPP = MAXN1 * MAXN1 * even_up<MAXN1>();
+    __shared__ __align__(16) float s_q[MAXPP];
+    __shared__ __align__(16) float s_w[MAXPP];
     __shared__ float s_p[3][MAXN1];
     __shared__ int s_item, s_mode;
     const int tid = threadIdx.x;
@@ -405,6 +425,7 @@ __global__ void __launch_bounds__(FT, 2) far_mixed(const __grid_constant__ Work 
         const Fields &a = w.sys[it.y >> 16];
         const int b = it.x, orb = it.y & 0xffff;
         const int n1 = a.n1, P = a.P;
+        const int n1p = n1 + (n1 & 1), Pp = n1 * n1 * n1p;
         const int f0 = a.far_off[b], f1 = a.far_off[b + 1];
         if (f0 == f1) continue;
         const int bn = a.batch_node[b];
@@ -417,7 +438,8 @@ __global__ void __launch_bounds__(FT, 2) far_mixed(const __grid_constant__ Work 
         const float *qh = a.qhat32 + (long)orb * a.nslots * P;
         for (int base = tb; base < te; base += FT * NT) {
             const bool warp_busy = base + NT * (tid & ~31) < te;
-            float tx[NT], ty[NT], tz[NT], fi[NT], sum[NT], cmp[NT];
+            float tx[NT], ty[NT], tz[NT], sum[NT], cmp[NT];
+            float2 nfi[NT];
 #pragma unroll
             for (int k = 0; k < NT; k++) {
                 const int i = base + NT * tid + k;
@@ -425,7 +447,7 @@ __global__ void __launch_bounds__(FT, 2) far_mixed(const __grid_constant__ Work 
                 tx[k] = v ? (float)(a.tx[i] - cb[0]) * scf : 0.f;
                 ty[k] = v ? (float)(a.ty[i] - cb[1]) * scf : 0.f;
                 tz[k] = v ? (float)(a.tz[i] - cb[2]) * scf : 0.f;
-                fi[k] = v ? ft[i] : 0.f;
+                nfi[k] = dup2(v ? -ft[i] : 0.f);
                 sum[k] = 0.f;
                 cmp[k] = 0.f;
             }
@@ -435,7 +457,13 @@ __global__ void __launch_bounds__(FT, 2) far_mixed(const __grid_constant__ Work 
                 __syncthreads();
                 const float *qs = qh + (long)slot * P;
                 const float *ws = a.what32 + (long)slot * P;
-                for (int k = tid; k < P; k += FT) s_qw[k] = make_float2(qs[k], ws[k]);
+                for (int k = tid; k < Pp; k += FT) {
+                    const int row = k / n1p, k3 = k - row * n1p;
+                    const bool real = k3 < n1;
+                    const int src = row * n1 + (real ? k3 : 0);
+                    s_q[k] = real ? qs[src] : 0.f;
+                    s_w[k] = real ? ws[src] : 0.f;
+                }
                 if (tid < 3 * n1) {
                     const int d = tid / n1, m = tid - d * n1;
                     const double cbd = d == 0 ? cb[0] : (d == 1 ? cb[1] : cb[2]);
@@ -455,8 +483,10 @@ __global__ void __launch_bounds__(FT, 2) far_mixed(const __grid_constant__ Work 
                 __syncthreads();
                 const int mode = s_mode;
                 if (mode == 2 || !warp_busy) continue;
-                if (mode == 1) far_cluster<KERN, SS, false, MAXN1, NT>(s_qw, s_p, n1, tx, ty, tz, fi, sum, cmp);
-                else far_cluster<KERN, SS, true, MAXN1, NT>(s_qw, s_p, n1, tx, ty, tz, fi, sum, cmp);
+                if (mode == 1)
+                    far_cluster<KERN, SS, false, MAXN1, NT>(s_q, s_w, s_p, n1, tx, ty, tz, nfi, sum, cmp);
+                else
+                    far_cluster<KERN, SS, true, MAXN1, NT>(s_q, s_w, s_p, n1, tx, ty, tz, nfi, sum, cmp);
             }
 #pragma unroll
             for (int k = 0; k < NT; k++) {
@@ -469,62 +499,72 @@ __global__ void __launch_bounds__(FT, 2) far_mixed(const __grid_constant__ Work 
 
 // ---------------------------------------------------------------------------
 // Orbital-group kernels (Yukawa, mixed precision): one item = (batch, group of
-// OG orbitals).  Per pair the differences, r^2, rsqrt and r are computed once
-// for the group; each orbital then adds exp2(-k_o log2(e) r) * rinv * c.
-// Coordinates are translated to the batch center but not scaled (each orbital
-// has its own k).  Charges are staged [source][orbital] so four orbitals come
-// in one 16-byte shared-memory read.  Orbitals past the last one of the
-// request have zero charges and are not written.
+// OG orbitals).  Per two sources (or two proxy points) the differences, r^2,
+// rsqrt and r are formed once for the group in packed operations; each orbital
+// then adds exp2(-k_o log2(e) r) * rinv * c with its own k (the constant
+// split hi + lo).  Coordinates are translated to the batch center but not
+// scaled (each orbital has its own k).  Charges are staged as float4
+// {q(o, j), q(o, j+1), q(o+1, j), q(o+1, j+1)} per (pair of sources, pair of
+// orbitals), so one 16-byte shared read serves four (pair, orbital) terms.
+// Orbitals past the last one of the request have zero charges and are not
+// written.
 // ---------------------------------------------------------------------------
 constexpr int GTILE = 256;   // sources per group tile
 
+__device__ __forceinline__ int q4_pos(int j, int o, int og) {   // float index of q(o, j) in the staged layout
+    return (((j >> 1) * (og >> 1) + (o >> 1)) << 2) + ((o & 1) << 1) + (j & 1);
+}
+
+// Group tile rows: 0..2 negated coordinates (batch-relative, or hi parts of
+// the absolute splits), 3 weight, 4..6 negated lo parts (PRECISE).
 template <bool SS, bool MASK, bool PRECISE, int OG>
-__device__ __forceinline__ void group_tile(const float4 *__restrict__ s_xyzw, const float4 *__restrict__ s_lo,
-                                           const float4 *__restrict__ s_q4, int cnt, float tx, float ty,
-                                           float tz, float lx, float ly, float lz, const float (&fi)[OG],
-                                           const float (&kc)[OG], const float (&kl)[OG], float (&sum)[OG],
-                                           float (&cmp)[OG]) {
-    for (int j0 = 0; j0 < cnt; j0 += KCHUNK) {
-        const int j1 = min(j0 + KCHUNK, cnt);
-        float part[OG];
+__device__ __forceinline__ void group_tile(const float (*__restrict__ s)[GTILE], const float4 *__restrict__ s_q4,
+                                           int cnt2, float2 tx, float2 ty, float2 tz, float2 lx, float2 ly,
+                                           float2 lz, const float2 (&nfi)[OG], const float2 (&kc)[OG],
+                                           const float2 (&kl)[OG], float (&sum)[OG], float (&cmp)[OG]) {
+    for (int j0 = 0; j0 < cnt2; j0 += KCHUNK) {
+        const int j1 = min(j0 + KCHUNK, cnt2);
+        float2 part[OG];
 #pragma unroll
-        for (int o = 0; o < OG; o++) part[o] = 0.f;
+        for (int o = 0; o < OG; o++) part[o] = make_float2(0.f, 0.f);
 #pragma unroll 2
-        for (int j = j0; j < j1; j++) {
-            const float4 sj = s_xyzw[j];
-            float dx = tx - sj.x, dy = ty - sj.y, dz = tz - sj.z;
-            if (PRECISE) {
-                const float4 sl = s_lo[j];
-                dx += lx - sl.x;
-                dy += ly - sl.y;
-                dz += lz - sl.z;
+        for (int j = j0; j < j1; j += 2) {
+            float2 dx = add2(tx, lds2(s[0] + j)), dy = add2(ty, lds2(s[1] + j)), dz = add2(tz, lds2(s[2] + j));
+            if constexpr (PRECISE) {
+                dx = add2(dx, add2(lx, lds2(s[4] + j)));
+                dy = add2(dy, add2(ly, lds2(s[5] + j)));
+                dz = add2(dz, add2(lz, lds2(s[6] + j)));
             }
-            const float r2 = fmaf(dx, dx, fmaf(dy, dy, dz * dz));
-            float rinv = rsqrt_mufu(r2);
-            if (MASK) rinv = r2 > 0.f ? rinv : 0.f;
-            const float r = r2 * rinv;
+            const float2 wv = lds2(s[3] + j);
+            const float2 r2 = fma2(dx, dx, fma2(dy, dy, mul2(dz, dz)));
+            float2 rinv = rsqrt2(r2);
+            if (MASK) {
+                rinv.x = r2.x > 0.f ? rinv.x : 0.f;
+                rinv.y = r2.y > 0.f ? rinv.y : 0.f;
+            }
+            const float2 r = mul2(r2, rinv);
 #pragma unroll
-            for (int o4 = 0; o4 < OG / 4; o4++) {
-                const float4 q4 = s_q4[j * (OG / 4) + o4];
-                const float qv[4] = {q4.x, q4.y, q4.z, q4.w};
+            for (int o2 = 0; o2 < OG / 2; o2++) {
+                const float4 q4 = s_q4[(j >> 1) * (OG / 2) + o2];
 #pragma unroll
-                for (int u = 0; u < 4; u++) {
-                    const int o = 4 * o4 + u;
+                for (int u = 0; u < 2; u++) {
+                    const int o = 2 * o2 + u;
+                    const float2 q = u ? make_float2(q4.z, q4.w) : make_float2(q4.x, q4.y);
                     // exponent -k log2(e) r with the constant split hi + lo
-                    const float g = ex2_mufu(fmaf(kc[o], r, kl[o] * r)) * rinv;
-                    part[o] = fmaf(g, SS ? fmaf(-fi[o], sj.w, qv[u]) : qv[u], part[o]);
+                    const float2 g = mul2(ex2pos2(fma2(kc[o], r, mul2(kl[o], r))), rinv);
+                    part[o] = fma2(g, SS ? fma2(nfi[o], wv, q) : q, part[o]);
                 }
             }
         }
 #pragma unroll
-        for (int o = 0; o < OG; o++) kahan_add(sum[o], cmp[o], part[o]);
+        for (int o = 0; o < OG; o++) kahan_add(sum[o], cmp[o], part[o].x + part[o].y);
     }
 }
 
 template <bool SS, int OG, int PASS>
 __global__ void __launch_bounds__(FT, 2) near_group(const __grid_constant__ Work w) {
-    __shared__ float4 s_xyzw[GTILE];
-    __shared__ float4 s_lo[GTILE];
+    constexpr int NR = PASS == 1 ? 7 : 4;
+    __shared__ __align__(16) float s_src[NR][GTILE];
     __shared__ float4 s_q4[GTILE * OG / 4];
     __shared__ int s_item;
     const int tid = threadIdx.x;
@@ -537,13 +577,16 @@ __global__ void __launch_bounds__(FT, 2) near_group(const __grid_constant__ Work
         const int bn = a.batch_node[b];
         const int tb = a.tbegin[bn], te = a.tend[bn];
         const double cbx = a.tcenter[3L * bn], cby = a.tcenter[3L * bn + 1], cbz = a.tcenter[3L * bn + 2];
-        float kc[OG], kl[OG];
+        float2 kc[OG], kl[OG];
         float kmin = 3.4e38f;
 #pragma unroll
         for (int o = 0; o < OG; o++) {
             const int orb = g0 + o;
             const double k2 = orb < a.norb ? -a.kp64[orb] * LOG2E : 0.0;   // -k log2(e)
-            split_f32(k2, kc[o], kl[o]);
+            float h, l;
+            split_f32(k2, h, l);
+            kc[o] = dup2(h);
+            kl[o] = dup2(l);
             if (orb < a.norb) kmin = fminf(kmin, a.kc32[orb]);
         }
         const int r0 = a.rng_off[b], r1 = a.rng_off[b + 1];
@@ -551,22 +594,27 @@ __global__ void __launch_bounds__(FT, 2) near_group(const __grid_constant__ Work
             const int i = base + tid;
             const bool v = i < te;
             const bool warp_busy = base + (tid & ~31) < te;
-            float tx, ty, tz, lx = 0.f, ly = 0.f, lz = 0.f;
+            float2 tx, ty, tz, lx = dup2(0.f), ly = dup2(0.f), lz = dup2(0.f);
             if (PASS == 1) {  // absolute hi/lo splits (see near_tile)
                 const float4 h = v ? a.thi[i] : make_float4(0.f, 0.f, 0.f, 0.f);
                 const float4 l = v ? a.tlo[i] : make_float4(0.f, 0.f, 0.f, 0.f);
-                tx = h.x; ty = h.y; tz = h.z;
-                lx = l.x; ly = l.y; lz = l.z;
+                tx = dup2(h.x);
+                ty = dup2(h.y);
+                tz = dup2(h.z);
+                lx = dup2(l.x);
+                ly = dup2(l.y);
+                lz = dup2(l.z);
             } else {
-                tx = v ? (float)(a.tx[i] - cbx) : 0.f;
-                ty = v ? (float)(a.ty[i] - cby) : 0.f;
-                tz = v ? (float)(a.tz[i] - cbz) : 0.f;
+                tx = dup2(v ? (float)(a.tx[i] - cbx) : 0.f);
+                ty = dup2(v ? (float)(a.ty[i] - cby) : 0.f);
+                tz = dup2(v ? (float)(a.tz[i] - cbz) : 0.f);
             }
-            float fi[OG], sum[OG], cmp[OG];
+            float2 nfi[OG];
+            float sum[OG], cmp[OG];
 #pragma unroll
             for (int o = 0; o < OG; o++) {
                 const int orb = g0 + o;
-                fi[o] = (v && orb < a.norb) ? a.ft32[(long)orb * a.nt + i] : 0.f;
+                nfi[o] = dup2((v && orb < a.norb) ? -a.ft32[(long)orb * a.nt + i] : 0.f);
                 sum[o] = 0.f;
                 cmp[o] = 0.f;
             }
@@ -578,37 +626,40 @@ __global__ void __launch_bounds__(FT, 2) near_group(const __grid_constant__ Work
                 const int rb = range_begin(r);
                 for (int t0 = rb; t0 < r.y; t0 += GTILE) {
                     const int cnt = min(GTILE, r.y - t0);
+                    const int cnt2 = (cnt + 1) & ~1;
                     __syncthreads();
-                    for (int j = tid; j < cnt; j += FT) {
-                        const int jj = t0 + j;
-                        float4 sa, sb;
-                        if (PASS == 1) {
-                            sa = a.shi[jj];
-                            sb = a.slo[jj];
+                    for (int j = tid; j < cnt2; j += FT) {
+                        const bool real = j < cnt;
+                        const int jj = t0 + (real ? j : 0);   // padding: a copy of the first source
+                        if constexpr (PASS == 1) {
+                            const float4 h = a.shi[jj], l = a.slo[jj];
+                            s_src[0][j] = -h.x;
+                            s_src[1][j] = -h.y;
+                            s_src[2][j] = -h.z;
+                            s_src[4][j] = -l.x;
+                            s_src[5][j] = -l.y;
+                            s_src[6][j] = -l.z;
                         } else {
-                            sa.x = (float)(a.sx[jj] - cbx);
-                            sa.y = (float)(a.sy[jj] - cby);
-                            sa.z = (float)(a.sz[jj] - cbz);
-                            sb.x = sb.y = sb.z = 0.f;
+                            s_src[0][j] = -(float)(a.sx[jj] - cbx);
+                            s_src[1][j] = -(float)(a.sy[jj] - cby);
+                            s_src[2][j] = -(float)(a.sz[jj] - cbz);
                         }
-                        sa.w = a.w32[jj];
-                        sb.w = 0.f;
-                        s_xyzw[j] = sa;
-                        s_lo[j] = sb;
+                        s_src[3][j] = real ? a.w32[jj] : 0.f;
                     }
-                    for (int k = tid; k < cnt * OG; k += FT) {
-                        const int j = k / OG, o = k - j * OG;
+                    for (int k = tid; k < cnt2 * OG; k += FT) {   // orbital-major: coalesced global reads
+                        const int o = k / cnt2, j = k - o * cnt2;
                         const int orb = g0 + o;
-                        reinterpret_cast<float *>(s_q4)[k] = orb < a.norb ? a.q32[(long)orb * a.ns + t0 + j] : 0.f;
+                        reinterpret_cast<float *>(s_q4)[q4_pos(j, o, OG)] =
+                            (j < cnt && orb < a.norb) ? a.q32[(long)orb * a.ns + t0 + j] : 0.f;
                     }
                     __syncthreads();
                     if (!warp_busy) continue;
                     if (PASS == 1)
-                        group_tile<SS, true, true, OG>(s_xyzw, s_lo, s_q4, cnt, tx, ty, tz, lx, ly, lz, fi, kc, kl,
-                                                       sum, cmp);
+                        group_tile<SS, true, true, OG>(s_src, s_q4, cnt2, tx, ty, tz, lx, ly, lz, nfi, kc, kl, sum,
+                                                       cmp);
                     else
-                        group_tile<SS, false, false, OG>(s_xyzw, s_lo, s_q4, cnt, tx, ty, tz, lx, ly, lz, fi, kc,
-                                                         kl, sum, cmp);
+                        group_tile<SS, false, false, OG>(s_src, s_q4, cnt2, tx, ty, tz, lx, ly, lz, nfi, kc, kl, sum,
+                                                         cmp);
                 }
             }
             if (v) {
@@ -620,13 +671,72 @@ __global__ void __launch_bounds__(FT, 2) near_group(const __grid_constant__ Work
     }
 }
 
+// One staged proxy grid against one target for a group of orbitals (see
+// far_cluster for the padded innermost axis).
+template <bool SS, int MAXN1, int OG>
+__device__ __forceinline__ void far_group_cluster(const float4 *__restrict__ s_q4, const float *__restrict__ s_w,
+                                                  const float (*s_p)[MAXN1], int n1, float tx, float ty, float tz,
+                                                  const float2 (&nfi)[OG], const float2 (&kc)[OG],
+                                                  const float2 (&kl)[OG], float (&sum)[OG], float (&cmp)[OG]) {
+    constexpr int MH = even_up<MAXN1>() / 2;
+    const int n1p = n1 + (n1 & 1);
+    float2 dz2[MH];
+#pragma unroll
+    for (int m = 0; m < MH; m++) {
+        const float d0 = tz - s_p[2][2 * m < n1 ? 2 * m : 0];
+        const float d1 = tz - s_p[2][2 * m + 1 < n1 ? 2 * m + 1 : 0];
+        dz2[m] = make_float2(d0 * d0, d1 * d1);
+    }
+    int idx = 0;
+    for (int k1 = 0; k1 < n1; k1++) {
+        float2 part[OG];
+#pragma unroll
+        for (int o = 0; o < OG; o++) part[o] = make_float2(0.f, 0.f);
+        const float dx = tx - s_p[0][k1];
+        const float dx2 = dx * dx;
+        for (int k2 = 0; k2 < n1; k2++) {
+            const float dy = ty - s_p[1][k2];
+            const float2 rxy = dup2(fmaf(dy, dy, dx2));
+#pragma unroll
+            for (int m = 0; m < MH; m++) {
+                if (2 * m < n1) {
+                    const float2 r2 = add2(rxy, dz2[m]);
+                    const float2 rinv = rsqrt2(r2);
+                    const float2 rr = mul2(r2, rinv);
+                    const float2 wk = lds2(s_w + idx + 2 * m);
+#pragma unroll
+                    for (int o2 = 0; o2 < OG / 2; o2++) {
+                        const float4 q4 = s_q4[((idx >> 1) + m) * (OG / 2) + o2];
+#pragma unroll
+                        for (int u = 0; u < 2; u++) {
+                            const int o = 2 * o2 + u;
+                            const float2 q = u ? make_float2(q4.z, q4.w) : make_float2(q4.x, q4.y);
+                            const float2 g = mul2(ex2pos2(fma2(kc[o], rr, mul2(kl[o], rr))), rinv);
+                            part[o] = fma2(g, SS ? fma2(nfi[o], wk, q) : q, part[o]);
+                        }
+                    }
+                }
+            }
+            idx += n1p;
+        }
+#pragma unroll
+        for (int o = 0; o < OG; o++) kahan_add(sum[o], cmp[o], part[o].x + part[o].y);
+    }
+}
+
+// Dynamic shared memory of far_group: the staged charges (Pp * OG floats,
+// Pp = n1 * n1 * n1p) then the weights (Pp floats), for the largest grid of
+// the launch's systems (above 48 KB at degree 10 with 8 orbitals).
+__host__ __device__ constexpr size_t far_group_smem(int n1, int og) {
+    return sizeof(float) * (size_t)n1 * n1 * (n1 + (n1 & 1)) * (og + 1);
+}
+
 template <bool SS, int MAXN1, int OG>
 __global__ void __launch_bounds__(FT, 2) far_group(const __grid_constant__ Work w) {
-    constexpr int MAXP = MAXN1 * MAXN1 * MAXN1;
-    __shared__ float4 s_q4[MAXP * OG / 4];
-    __shared__ float s_w[MAXP];
+    extern __shared__ __align__(16) float s_dyn[];
     __shared__ float s_p[3][MAXN1];
     __shared__ int s_item;
+    float4 *s_q4 = reinterpret_cast<float4 *>(s_dyn);
     const int tid = threadIdx.x;
     for (;;) {
         const int item = next_item(w.queue, &s_item);
@@ -635,14 +745,21 @@ __global__ void __launch_bounds__(FT, 2) far_group(const __grid_constant__ Work 
         const Fields &a = w.sys[it.y >> 16];
         const int b = it.x, g0 = it.y & 0xffff;
         const int n1 = a.n1, P = a.P;
+        const int n1p = n1 + (n1 & 1), Pp = n1 * n1 * n1p;
+        const float *s_w = s_dyn + (size_t)Pp * OG;   // Pp * OG is a multiple of 4: float4 aligned
         const int f0 = a.far_off[b], f1 = a.far_off[b + 1];
         if (f0 == f1) continue;
         const int bn = a.batch_node[b];
         const int tb = a.tbegin[bn], te = a.tend[bn];
         const double cb[3] = {a.tcenter[3L * bn], a.tcenter[3L * bn + 1], a.tcenter[3L * bn + 2]};
-        float kc[OG], kl[OG];
+        float2 kc[OG], kl[OG];
 #pragma unroll
-        for (int o = 0; o < OG; o++) split_f32((g0 + o) < a.norb ? -a.kp64[g0 + o] * LOG2E : 0.0, kc[o], kl[o]);
+        for (int o = 0; o < OG; o++) {
+            float h, l;
+            split_f32((g0 + o) < a.norb ? -a.kp64[g0 + o] * LOG2E : 0.0, h, l);
+            kc[o] = dup2(h);
+            kl[o] = dup2(l);
+        }
         for (int base = tb; base < te; base += FT) {
             const int i = base + tid;
             const bool v = i < te;
@@ -650,11 +767,12 @@ __global__ void __launch_bounds__(FT, 2) far_group(const __grid_constant__ Work 
             const float tx = v ? (float)(a.tx[i] - cb[0]) : 0.f;
             const float ty = v ? (float)(a.ty[i] - cb[1]) : 0.f;
             const float tz = v ? (float)(a.tz[i] - cb[2]) : 0.f;
-            float fi[OG], sum[OG], cmp[OG];
+            float2 nfi[OG];
+            float sum[OG], cmp[OG];
 #pragma unroll
             for (int o = 0; o < OG; o++) {
                 const int orb = g0 + o;
-                fi[o] = (v && orb < a.norb) ? a.ft32[(long)orb * a.nt + i] : 0.f;
+                nfi[o] = dup2((v && orb < a.norb) ? -a.ft32[(long)orb * a.nt + i] : 0.f);
                 sum[o] = 0.f;
                 cmp[o] = 0.f;
             }
@@ -662,13 +780,17 @@ __global__ void __launch_bounds__(FT, 2) far_group(const __grid_constant__ Work 
                 const int slot = a.node_slot[a.far_list[e]];
                 const double *gm = a.geom + 6L * slot;
                 __syncthreads();
-                for (int k = tid; k < P * OG; k += FT) {
-                    const int kk = k / OG, o = k - kk * OG;
+                for (int k = tid; k < Pp * OG; k += FT) {   // orbital-major: coalesced global reads
+                    const int o = k / Pp, kk = k - o * Pp;
+                    const int row = kk / n1p, k3 = kk - row * n1p;
                     const int orb = g0 + o;
-                    reinterpret_cast<float *>(s_q4)[k] =
-                        orb < a.norb ? a.qhat32[((long)orb * a.nslots + slot) * P + kk] : 0.f;
+                    reinterpret_cast<float *>(s_q4)[q4_pos(kk, o, OG)] =
+                        (k3 < n1 && orb < a.norb) ? a.qhat32[((long)orb * a.nslots + slot) * P + row * n1 + k3] : 0.f;
                 }
-                for (int k = tid; k < P; k += FT) s_w[k] = a.what32[(long)slot * P + k];
+                for (int k = tid; k < Pp; k += FT) {
+                    const int row = k / n1p, k3 = k - row * n1p;
+                    s_dyn[(size_t)Pp * OG + k] = k3 < n1 ? a.what32[(long)slot * P + row * n1 + k3] : 0.f;
+                }
                 if (tid < 3 * n1) {
                     const int d = tid / n1, m = tid - d * n1;
                     const double cbd = d == 0 ? cb[0] : (d == 1 ? cb[1] : cb[2]);
@@ -676,47 +798,7 @@ __global__ void __launch_bounds__(FT, 2) far_group(const __grid_constant__ Work 
                 }
                 __syncthreads();
                 if (!warp_busy) continue;
-                float dz2[MAXN1];
-#pragma unroll
-                for (int m = 0; m < MAXN1; m++) {
-                    const float d = tz - s_p[2][m < n1 ? m : 0];
-                    dz2[m] = d * d;
-                }
-                int idx = 0;
-                for (int k1 = 0; k1 < n1; k1++) {
-                    float part[OG];
-#pragma unroll
-                    for (int o = 0; o < OG; o++) part[o] = 0.f;
-                    const float dx = tx - s_p[0][k1];
-                    const float dx2 = dx * dx;
-                    for (int k2 = 0; k2 < n1; k2++) {
-                        const float dy = ty - s_p[1][k2];
-                        const float rxy = fmaf(dy, dy, dx2);
-#pragma unroll
-                        for (int k3 = 0; k3 < MAXN1; k3++) {
-                            if (k3 < n1) {
-                                const float r2 = rxy + dz2[k3];
-                                const float rinv = rsqrt_mufu(r2);
-                                const float rr = r2 * rinv;
-                                const float wk = s_w[idx + k3];
-#pragma unroll
-                                for (int o4 = 0; o4 < OG / 4; o4++) {
-                                    const float4 q4 = s_q4[(idx + k3) * (OG / 4) + o4];
-                                    const float qv[4] = {q4.x, q4.y, q4.z, q4.w};
-#pragma unroll
-                                    for (int u = 0; u < 4; u++) {
-                                        const int o = 4 * o4 + u;
-                                        const float g = ex2_mufu(fmaf(kc[o], rr, kl[o] * rr)) * rinv;
-                                        part[o] = fmaf(g, SS ? fmaf(-fi[o], wk, qv[u]) : qv[u], part[o]);
-                                    }
-                                }
-                            }
-                        }
-                        idx += n1;
-                    }
-#pragma unroll
-                    for (int o = 0; o < OG; o++) kahan_add(sum[o], cmp[o], part[o]);
-                }
+                far_group_cluster<SS, MAXN1, OG>(s_q4, s_w, s_p, n1, tx, ty, tz, nfi, kc, kl, sum, cmp);
             }
             if (v) {
 #pragma unroll
@@ -905,99 +987,151 @@ __global__ void epilogue(const double *__restrict__ nearv, const double *__restr
 }
 
 template <typename K>
-int occupancy_grid(K kern, int *grid) {
+int occupancy_grid(K kern, int *grid, size_t smem = 0) {
     int dev = 0, sms = 0, per = 0;
     TAGI_CUDA(cudaGetDevice(&dev));
     TAGI_CUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
-    TAGI_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, kern, FT, 0));
+    TAGI_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, kern, FT, smem));
     *grid = sms * (per > 0 ? per : 1);
     return TAGI_OK;
 }
 
+// Persistent launch: grid = resident CTAs (at most one per work item).  smem
+// bytes of dynamic shared memory; above the 48 KB default the kernel's limit
+// is raised first.
 template <typename K>
-int launch_persistent(K kern, const Work &w, cudaStream_t s) {
+int launch_persistent(K kern, const Work &w, cudaStream_t s, size_t smem = 0) {
     if (w.nitems == 0) return TAGI_OK;
+    if (smem > 48 * 1024)
+        TAGI_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
     int grid = 0;
-    TAGI_TRY(occupancy_grid(kern, &grid));
+    TAGI_TRY(occupancy_grid(kern, &grid, smem));
     if (grid > w.nitems) grid = w.nitems;
     if (grid < 1) grid = 1;
-    launch(kern, grid, FT, 0, s, w);
+    launch(kern, grid, FT, smem, s, w);
     TAGI_LAUNCH_CHECK();
     return TAGI_OK;
 }
 
 // ---------------------------------------------------------------------------
-// Pair-throughput ceiling: the near/far inner loops' arithmetic with operands
-// already in shared memory and registers and no global traffic.  The field
-// kernels' roofline fraction is measured against this, live, on the same GPU.
+// Loop ceilings: the near/far inner loops' arithmetic with operands already
+// in shared memory and registers and no global traffic, measured live on the
+// same GPU.  The ratio of a field kernel's pair rate to its loop's ceiling is
+// its loop efficiency (staging, scheduling and tails); the hardware roofline
+// is the per-pipe rate (tagi_pipe_rates).
 // ---------------------------------------------------------------------------
 template <int KERN, bool SS>
 __global__ void __launch_bounds__(FT) pair_peak_near(int reps, float *out) {
-    __shared__ float4 s_a[NTILE];
-    __shared__ float4 s_b[NTILE];
+    __shared__ __align__(16) float s[5][NTILE];
     for (int j = threadIdx.x; j < NTILE; j += FT) {
-        float v = (float)((j * 37) % 101) * 0.01f - 0.5f;
-        s_a[j] = make_float4(v, 0.3f * v + 0.1f, 0.7f - v, 0.5f + 0.001f * j);
-        s_b[j] = make_float4(0.f, 0.f, 0.f, 0.25f);
+        const float v = (float)((j * 37) % 101) * 0.01f - 0.5f;
+        s[0][j] = -v;
+        s[1][j] = -(0.3f * v + 0.1f);
+        s[2][j] = -(0.7f - v);
+        s[3][j] = 0.5f + 0.001f * j;
+        s[4][j] = 0.25f;
     }
     __syncthreads();
-    float tx[2], ty[2], tz[2], fi[2];
+    float2 tx[2], ty[2], tz[2], z2[2], nfi[2];
     float sum[2] = {0.f, 0.f}, cmp[2] = {0.f, 0.f};
     for (int k = 0; k < 2; k++) {
-        tx[k] = 0.01f * (threadIdx.x & 31) + 0.003f * k;
-        ty[k] = 0.02f;
-        tz[k] = -0.03f * (threadIdx.x >> 5);
-        fi[k] = 0.3f;
+        tx[k] = dup2(0.01f * (threadIdx.x & 31) + 0.003f * k);
+        ty[k] = dup2(0.02f);
+        tz[k] = dup2(-0.03f * (threadIdx.x >> 5));
+        z2[k] = dup2(0.f);
+        nfi[k] = dup2(-0.3f);
     }
     for (int r = 0; r < reps; r++)
-        near_tile<KERN, SS, false, false, 2>(s_a, s_b, NTILE, tx, ty, tz, nullptr, 1.f, fi, sum, cmp);
+        near_tile<KERN, SS, false, false, 2>(s, NTILE, tx, ty, tz, z2, z2, z2, dup2(1.f), nfi, sum, cmp);
     out[blockIdx.x * FT + threadIdx.x] = sum[0] + sum[1] - cmp[0] - cmp[1];
 }
 
 template <int KERN, bool SS>
 __global__ void __launch_bounds__(FT) pair_peak_far(int reps, float *out) {
     constexpr int N1 = 8;
-    __shared__ float2 s_qw[N1 * N1 * N1];
+    __shared__ __align__(16) float s_q[N1 * N1 * N1];
+    __shared__ __align__(16) float s_w[N1 * N1 * N1];
     __shared__ float s_p[3][N1];
-    for (int k = threadIdx.x; k < N1 * N1 * N1; k += FT) s_qw[k] = make_float2(0.5f + 0.001f * k, 0.25f);
+    for (int k = threadIdx.x; k < N1 * N1 * N1; k += FT) {
+        s_q[k] = 0.5f + 0.001f * k;
+        s_w[k] = 0.25f;
+    }
     if (threadIdx.x < 3 * N1) s_p[threadIdx.x / N1][threadIdx.x % N1] = 1.0f + 0.1f * threadIdx.x;
     __syncthreads();
-    float tx[2], ty[2], tz[2], fi[2], sum[2] = {0.f, 0.f}, cmp[2] = {0.f, 0.f};
+    float tx[2], ty[2], tz[2], sum[2] = {0.f, 0.f}, cmp[2] = {0.f, 0.f};
+    float2 nfi[2];
     for (int k = 0; k < 2; k++) {
         tx[k] = 0.01f * (threadIdx.x & 31) + 0.003f * k;
         ty[k] = 0.02f;
         tz[k] = -0.03f * (threadIdx.x >> 5);
-        fi[k] = 0.3f;
+        nfi[k] = dup2(-0.3f);
     }
-    for (int r = 0; r < reps; r++) far_cluster<KERN, SS, true, N1, 2>(s_qw, s_p, N1, tx, ty, tz, fi, sum, cmp);
+    for (int r = 0; r < reps; r++)
+        far_cluster<KERN, SS, true, N1, 2>(s_q, s_w, s_p, N1, tx, ty, tz, nfi, sum, cmp);
     out[blockIdx.x * FT + threadIdx.x] = sum[0] + sum[1] - cmp[0] - cmp[1];
 }
 
-// Yukawa orbital groups: group_tile over one staged tile, 8 orbitals per
-// pair geometry; counted per (pair, orbital).
+// Yukawa orbital groups, 8 orbitals per pair geometry; counted per (pair, orbital).
 template <bool SS>
 __global__ void __launch_bounds__(FT, 2) pair_peak_near_group(int reps, float *out) {
     constexpr int OG = 8;
-    __shared__ float4 s_xyzw[GTILE];
-    __shared__ float4 s_lo[GTILE];
+    __shared__ __align__(16) float s[4][GTILE];
     __shared__ float4 s_q4[GTILE * OG / 4];
     for (int j = threadIdx.x; j < GTILE; j += FT) {
         const float v = (float)((j * 37) % 101) * 0.01f - 0.5f;
-        s_xyzw[j] = make_float4(v, 0.3f * v + 0.1f, 0.7f - v, 0.25f);
-        s_lo[j] = make_float4(0.f, 0.f, 0.f, 0.f);
+        s[0][j] = -v;
+        s[1][j] = -(0.3f * v + 0.1f);
+        s[2][j] = -(0.7f - v);
+        s[3][j] = 0.25f;
     }
     for (int k = threadIdx.x; k < GTILE * OG; k += FT) reinterpret_cast<float *>(s_q4)[k] = 0.5f + 0.001f * k;
     __syncthreads();
-    const float tx = 0.01f * (threadIdx.x & 31), ty = 0.02f, tz = -0.03f * (threadIdx.x >> 5);
-    float fi[OG], kc[OG], kl[OG], sum[OG], cmp[OG];
+    const float2 tx = dup2(0.01f * (threadIdx.x & 31)), ty = dup2(0.02f), tz = dup2(-0.03f * (threadIdx.x >> 5));
+    float2 nfi[OG], kc[OG], kl[OG];
+    float sum[OG], cmp[OG];
 #pragma unroll
     for (int o = 0; o < OG; o++) {
-        fi[o] = 0.3f;
-        split_f32(-(0.5 + 0.3 * o) * LOG2E, kc[o], kl[o]);
+        float h, l;
+        split_f32(-(0.5 + 0.3 * o) * LOG2E, h, l);
+        kc[o] = dup2(h);
+        kl[o] = dup2(l);
+        nfi[o] = dup2(-0.3f);
+        sum[o] = cmp[o] = 0.f;
+    }
+    const float2 z = dup2(0.f);
+    for (int r = 0; r < reps; r++)
+        group_tile<SS, false, false, OG>(s, s_q4, GTILE, tx, ty, tz, z, z, z, nfi, kc, kl, sum, cmp);
+    float acc = 0.f;
+#pragma unroll
+    for (int o = 0; o < OG; o++) acc += sum[o] - cmp[o];
+    out[blockIdx.x * FT + threadIdx.x] = acc;
+}
+
+// Yukawa orbital groups in the far field: one degree-7 proxy grid, 8 orbitals.
+template <bool SS>
+__global__ void __launch_bounds__(FT, 2) pair_peak_far_group(int reps, float *out) {
+    constexpr int OG = 8, N1 = 8, PP = N1 * N1 * N1;
+    __shared__ float4 s_q4[PP * OG / 4];
+    __shared__ __align__(16) float s_w[PP];
+    __shared__ float s_p[3][N1];
+    for (int k = threadIdx.x; k < PP * OG; k += FT) reinterpret_cast<float *>(s_q4)[k] = 0.5f + 0.001f * k;
+    for (int k = threadIdx.x; k < PP; k += FT) s_w[k] = 0.25f;
+    if (threadIdx.x < 3 * N1) s_p[threadIdx.x / N1][threadIdx.x % N1] = 1.0f + 0.1f * threadIdx.x;
+    __syncthreads();
+    const float tx = 0.01f * (threadIdx.x & 31), ty = 0.02f, tz = -0.03f * (threadIdx.x >> 5);
+    float2 nfi[OG], kc[OG], kl[OG];
+    float sum[OG], cmp[OG];
+#pragma unroll
+    for (int o = 0; o < OG; o++) {
+        float h, l;
+        split_f32(-(0.5 + 0.3 * o) * LOG2E, h, l);
+        kc[o] = dup2(h);
+        kl[o] = dup2(l);
+        nfi[o] = dup2(-0.3f);
         sum[o] = cmp[o] = 0.f;
     }
     for (int r = 0; r < reps; r++)
-        group_tile<SS, false, false, OG>(s_xyzw, s_lo, s_q4, GTILE, tx, ty, tz, 0.f, 0.f, 0.f, fi, kc, kl, sum, cmp);
+        far_group_cluster<SS, N1, OG>(s_q4, s_w, s_p, N1, tx, ty, tz, nfi, kc, kl, sum, cmp);
     float acc = 0.f;
 #pragma unroll
     for (int o = 0; o < OG; o++) acc += sum[o] - cmp[o];
@@ -1008,20 +1142,23 @@ template <int KERN, bool SS>
 int launch_pair_peak(int variant, int grid, int reps, float *out, cudaStream_t s) {
     if (variant == 0) launch(pair_peak_near<KERN, SS>, grid, FT, 0, s, reps, out);
     else if (variant == 1) launch(pair_peak_far<KERN, SS>, grid, FT, 0, s, reps, out);
-    else launch(pair_peak_near_group<SS>, grid, FT, 0, s, reps, out);
+    else if (variant == 2) launch(pair_peak_near_group<SS>, grid, FT, 0, s, reps, out);
+    else launch(pair_peak_far_group<SS>, grid, FT, 0, s, reps, out);
     TAGI_LAUNCH_CHECK();
     return TAGI_OK;
 }
 
 template <int KERN, bool SS>
 int run_pair_peak(int variant, double *pairs_per_s, cudaStream_t s) {
-    if (variant < 0 || variant > 2) return set_error(TAGI_ERR_ARG, "pair peak variant %d (0 near, 1 far, 2 near group)", variant);
-    if (variant == 2 && KERN != KERNEL_YUKAWA)
+    if (variant < 0 || variant > 3)
+        return set_error(TAGI_ERR_ARG, "pair peak variant %d (0 near, 1 far, 2 near group, 3 far group)", variant);
+    if (variant >= 2 && KERN != KERNEL_YUKAWA)
         return set_error(TAGI_ERR_UNSUPPORTED, "orbital-group kernels are Yukawa only");
     int grid = 0;
     if (variant == 0) TAGI_TRY(occupancy_grid(pair_peak_near<KERN, SS>, &grid));
     else if (variant == 1) TAGI_TRY(occupancy_grid(pair_peak_far<KERN, SS>, &grid));
-    else TAGI_TRY(occupancy_grid(pair_peak_near_group<SS>, &grid));
+    else if (variant == 2) TAGI_TRY(occupancy_grid(pair_peak_near_group<SS>, &grid));
+    else TAGI_TRY(occupancy_grid(pair_peak_far_group<SS>, &grid));
     Arena tmp;
     tmp.stream = s;
     float *out = nullptr;
@@ -1030,7 +1167,7 @@ int run_pair_peak(int variant, double *pairs_per_s, cudaStream_t s) {
     cudaEventCreate(&a);
     cudaEventCreate(&b);
     // pairs per repetition per thread: two targets x a tile, or one target x a tile x 8 orbitals
-    const int per_rep = variant == 0 ? 2 * NTILE : (variant == 1 ? 2 * 512 : GTILE * 8);
+    const int per_rep = variant == 0 ? 2 * NTILE : (variant == 1 ? 2 * 512 : (variant == 2 ? GTILE * 8 : 512 * 8));
     int reps = 16;
     float ms = 0.f;
     int rc = TAGI_OK;
@@ -1092,15 +1229,16 @@ int launch_fields(const SysCall *calls, const Fields *f, int nsys, const Schedul
         else TAGI_TRY(launch_persistent(near_group<SS, 4, 1>, wc, s));
         phase_mark(PH_NEAR_CLOSE, false, s);
         phase_mark(PH_FAR, true, s);
+        const size_t fsm = far_group_smem(sh.maxn1, sh.og);
         if (sh.maxn1 <= 4) {
-            if (g8) TAGI_TRY(launch_persistent(far_group<SS, 4, 8>, wf, s));
-            else TAGI_TRY(launch_persistent(far_group<SS, 4, 4>, wf, s));
+            if (g8) TAGI_TRY(launch_persistent(far_group<SS, 4, 8>, wf, s, fsm));
+            else TAGI_TRY(launch_persistent(far_group<SS, 4, 4>, wf, s, fsm));
         } else if (sh.maxn1 <= 8) {
-            if (g8) TAGI_TRY(launch_persistent(far_group<SS, 8, 8>, wf, s));
-            else TAGI_TRY(launch_persistent(far_group<SS, 8, 4>, wf, s));
+            if (g8) TAGI_TRY(launch_persistent(far_group<SS, 8, 8>, wf, s, fsm));
+            else TAGI_TRY(launch_persistent(far_group<SS, 8, 4>, wf, s, fsm));
         } else {
-            if (g8) TAGI_TRY(launch_persistent(far_group<SS, MAX_DEGREE + 1, 8>, wf, s));
-            else TAGI_TRY(launch_persistent(far_group<SS, MAX_DEGREE + 1, 4>, wf, s));
+            if (g8) TAGI_TRY(launch_persistent(far_group<SS, MAX_DEGREE + 1, 8>, wf, s, fsm));
+            else TAGI_TRY(launch_persistent(far_group<SS, MAX_DEGREE + 1, 4>, wf, s, fsm));
         }
         phase_mark(PH_FAR, false, s);
         return TAGI_OK;

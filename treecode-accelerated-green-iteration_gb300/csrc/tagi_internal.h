@@ -242,6 +242,7 @@ int direct_sum(int nt, const double *tx, const double *ty, const double *tz, con
                double kp, int singularity, int precision, cudaStream_t s);
 
 int pair_peak(int kernel, int singularity, int variant, double kp, double *pairs_per_s, cudaStream_t s);
+int pipe_rates(double *rates, cudaStream_t s);
 
 // mgs.cu / interp.cu
 int mgs_device(double *V, double *U, const double *W, int target, int npts, int nwave,
