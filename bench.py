@@ -1,42 +1,56 @@
 #!/usr/bin/env python
 """Benchmark of the GB300 treecode convolution path.
 
-Workload (default): the Coulomb Hartree convolution with singularity
-subtraction on a seeded synthetic ~1.5M-point mesh (4 nuclei in a 6 Bohr box,
-Z from {1,6,8}, order-7 cells, depth <= 7; density = 3 Gaussians per nucleus,
-exponents log-uniform in [0.1, 10]), mixed precision, degree 7, theta 0.7.
+Default workload (``--workload orbitals``): 32 Yukawa orbital convolutions
+with singularity subtraction on one seeded synthetic ~1M-point mesh (3 nuclei
+Z = 6, 7, 8, order-7 cells; psi_i random signed sums of 4 Gaussians on the
+nuclei, exponents log-uniform in [0.1, 10]; sources f_i = -2 V psi_i; k_i ~
+U[0.4, 3.0]), all 32 in one persistent launch per field pass in mixed
+precision, degree 7, theta 0.7, followed by the FP64 quadrature-weighted
+Gram-Schmidt of the 32 results psi_i' = conv_i / 4 pi in orbital order.
 
-One step = one full treecode convolution as one callTreedriver call does it:
-tree + batches + lists + weight charges (the plan), modified charges, near
-and far fields, epilogue -- inputs already resident in HBM.  ``value`` =
-convolutions/s over all ranks.  ``e2e`` = the same through the C ABI
-(tagi_BaryTreeInterface_ex) with pinned host buffers: host->device copies,
-device allocation and the device->host result copy are inside the timing.
+One step = what a Green-iteration sweep's convolution part does with its
+inputs resident in HBM: tree + batches + lists + weight charges (the plan),
+modified charges, near and far fields, epilogue for all 32 orbitals, then the
+Gram-Schmidt.  ``value`` = orbital convolutions/s over all ranks.  ``e2e`` =
+the same from pinned host buffers through the public one-shot call
+(tagi_treecode_batched, which builds its plan inside) and the Gram-Schmidt,
+with the host->device copies of mesh and orbitals and the device->host copy
+of the 32 results inside the timing.  ``vs_plain``: the plain FP64 path --
+one tagi_treecode_dev call per orbital (tree + convolution, leaves 500) --
+timed on orbitals 0 and 31 of the same mesh.
 
   python bench.py [--gpus N] [--steps K] [--warmup W] [--impl gb300|reference]
-                  [--workload hartree|orbitals|uneven|scf|mesh|twomesh]
+                  [--workload orbitals|hartree|uneven|scf|mesh|twomesh]
 
-``--workload uneven``: six independent synthetic systems (50k .. 2.5M points,
-4/8/8/16/32/64 orbitals, Yukawa with subtraction, k_i ~ U[0.4, 3]) convolved
-together, all orbitals of all systems in one persistent launch per field pass,
-the launch sequence captured once as a CUDA graph and replayed; leaf sizes and
-kernel shape chosen by the autotuner (untimed).  One step = one replay: one
-Green-iteration sweep's convolutions (plans reused, as Green iteration reuses
-them).  Compared with the plain path: one FP64 tagi_treecode_dev call per
-orbital (tree + convolution each, reference parameters: leaves 500).
+``--workload hartree``: one Coulomb Hartree convolution with subtraction on a
+~1.5M-point mesh (4 nuclei in a 6 Bohr box, 3 Gaussians per nucleus), mixed.
+``--workload uneven``: six independent systems (50k .. 2.5M points, 4..64
+orbitals) in one persistent launch per field pass, replayed as a CUDA graph,
+leaf sizes and kernel shape from the autotuner.  ``--workload mesh`` /
+``twomesh``: the ring molecule's two-level mesh built on the device / its
+two-mesh eigenvalue correction of 21 orbitals.  ``--workload scf``: the ring
+molecule's SCF, plain vs learned extrapolation.
 
-``--workload mesh``: the ring molecule's two-level mesh built on the device
-(refinement + coarse and fine points); ``--workload twomesh``: the two-mesh
-eigenvalue correction of 21 orbitals on that mesh.
+Roofline: the field kernels compute pairwise sums -- neither HBM nor the
+tensor cores bind them.  ``roofline`` reports the dominant kernel's rate
+against the hardware pipes it uses: FP32 lane operations, MUFU ex2 and MUFU
+rsqrt per unit of work (a pair interaction, or a pair-orbital for the
+orbital-group kernels; counted from the kernel's source), each pipe's rate
+measured live on this GPU (tagi_pipe_rates).  ``loop_efficiency`` is the rate
+against the kernel's own inner loop run from shared memory (tagi_pair_peak).
 
 ``--impl reference`` times the CPU FP64 restatement of the same treecode (the
-reference's BaryTree is not available) on the host cores, on a bounded sample
-of target batches per step, extrapolated by pair count.
+reference's BaryTree is not available) on the host cores: the plan once, then
+per step the fields of one orbital on a fixed stratified sample of target
+batches (the same sample the GPU arm's cpu_baseline uses), extrapolated by
+pair count.
 """
 import argparse
 import ctypes
 import importlib
 import json
+import math
 import os
 import statistics
 import subprocess
@@ -54,7 +68,31 @@ METRIC = "orbital convs/s at 1e-6 rel err; wall time to 1e-5 Ha SCF: chosen vs p
 UNIT = "convolutions/s"
 THETA, DEGREE = 0.7, 7
 LEAF = {"hartree": (2000, 2000), "orbitals": (2000, 2000)}
-PAIR_FLOPS = {"coulomb_ss": 14, "yukawa_ss": 15}  # FP32 pipe operations counted per pair in the near-tile loop
+PLAIN_LEAF = 500  # 500-point leaves, the tree parameters the reference's single-atom runs use
+CPU_SAMPLE_BATCHES = 48  # stratified target batches per CPU-baseline sample
+
+# FP32 lane operations, MUFU ex2 and MUFU rsqrt per unit of work of each
+# mixed-precision field kernel, counted from csrc/fields.cu (two lanes per
+# packed FADD2/FMUL2/FFMA2).  Unit: a pair interaction; for the orbital-group
+# kernels a (pair, orbital) interaction with OG orbitals per pair geometry.
+#   near_mixed  Coulomb SS: 3 differences + 3 for r^2 + (f_i e, q - f_i e w,
+#               accumulate); Yukawa SS: 6 + (r, 2^-r'/r', q - f_i w, accumulate)
+#   far_mixed   r^2 from per-axis squares (1 + 2/n1 for the row sums), then as
+#               the near loop
+#   near_group  per pair 3 + 3 + r (shared by OG orbitals); per orbital the
+#               split exponent (2), 2^x/r', q - f_i w, accumulate
+#   far_group   per pair r^2 + r (+ 2/n1); per orbital 5
+def field_ops(kernel, label, og=8, n1=8):
+    yuk = label.startswith("yukawa")
+    if kernel == "near_mixed":
+        return (10.0, 1.0, 1.0) if yuk else (9.0, 1.0, 1.0)
+    if kernel == "far_mixed":
+        return (5.0 + 2.0 / n1, 1.0, 1.0) if yuk else (4.0 + 2.0 / n1, 1.0, 1.0)
+    if kernel == "near_group":
+        return (5.0 + 7.0 / og, 1.0, 1.0 / og)
+    if kernel == "far_group":
+        return (5.0 + (2.0 + 2.0 / n1) / og, 1.0, 1.0 / og)
+    raise ValueError(kernel)
 
 
 def parse():
@@ -63,17 +101,20 @@ def parse():
     ap.add_argument("--steps", type=int, default=5)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
-    ap.add_argument("--workload", default="hartree", choices=["hartree", "orbitals", "uneven", "scf", "mesh", "twomesh"])
+    ap.add_argument("--workload", default="orbitals",
+                    choices=["orbitals", "hartree", "uneven", "scf", "mesh", "twomesh"])
     ap.add_argument("--scf-points", type=int, default=3_000_000, help="scf workload: mesh points")
     ap.add_argument("--scf-max-iter", type=int, default=60)
     ap.add_argument("--scf-orbitals", type=int, default=21, help="scf workload: orbitals (21 occupied)")
     ap.add_argument("--scf-mixing", type=float, default=0.3, help="scf workload: density mixing parameter")
     ap.add_argument("--scf-time-limit", type=float, default=1500.0, help="scf workload: seconds per run")
+    ap.add_argument("--scf-arms", default="plain,learned", help="scf workload: arms to run")
     ap.add_argument("--fp64-sample-systems", type=int, default=2,
                     help="uneven workload: systems whose plain FP64 one-call-per-orbital time is measured")
     ap.add_argument("--cpu-seconds", type=float, default=15.0,
-                    help="target CPU seconds of field work per CPU-baseline sample")
+                    help="target CPU seconds of field work per CPU-baseline sample (mesh/twomesh workloads)")
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-plain", action="store_true", help="skip the plain FP64 comparison")
     return ap.parse_args()
 
 
@@ -111,11 +152,46 @@ def make_workload(name):
         mesh, rho = syn.hartree_system(seed=2)
         return dict(mesh=mesh, values=rho[None, :], kparams=np.array([[1.0]]),
                     kernel=BT.Kernel.COULOMB, singularity=BT.Singularity.SUBTRACTION,
-                    label="coulomb_ss", desc="coulomb_hartree_ss_1.5M")
+                    label="coulomb_ss", desc="coulomb_hartree_ss_1.5M", mgs=False)
     mesh, F, k = syn.multi_orbital_system(seed=3, n_orb=32)
     return dict(mesh=mesh, values=F, kparams=k[:, None], kernel=BT.Kernel.YUKAWA,
                 singularity=BT.Singularity.SUBTRACTION, label="yukawa_ss",
-                desc="yukawa_32_orbitals_1M")
+                desc="yukawa_32_orbitals_1M_then_fp64_gram_schmidt", mgs=True)
+
+
+# ---------------------------------------------------------------------------
+# Hardware pipe roofline
+# ---------------------------------------------------------------------------
+def pipe_rates(L, nat, stream):
+    """Lane operations/s of FFMA, FFMA2, MUFU ex2, MUFU rsqrt on this GPU (tagi_pipe_rates)."""
+    r = (ctypes.c_double * 6)()
+    nat.check(L.tagi_pipe_rates(r, ctypes.c_void_p(stream.cuda_stream)))
+    return dict(ffma=r[0], ffma2=r[1], ex2=r[2], rsqrt=r[3], probe_mhz=r[4], sms=int(r[5]))
+
+
+def pipe_roofline(units, ms, ops, rates, clock_mhz):
+    """Roofline of a field kernel against the FP32 and MUFU pipes.
+
+    units: work units of the launch; ms: its duration; ops = (FP32 lane ops,
+    ex2, rsqrt) per unit; rates: measured lane-op rates.  MUFU ex2 and rsqrt
+    share one pipe, so their times add.  Returns the kernel's units/s, the
+    units/s the binding pipe allows, and each pipe's busy fraction."""
+    fp32 = max(rates["ffma"], rates["ffma2"])
+    t_fma = ops[0] / fp32
+    t_mufu = ops[1] / rates["ex2"] + ops[2] / rates["rsqrt"]
+    achieved = units / (ms * 1e-3)
+    peak = 1.0 / max(t_fma, t_mufu)
+    fr = {"fp32": achieved * t_fma, "mufu": achieved * t_mufu}
+    bound = max(fr, key=fr.get)
+    per_clk = None
+    if clock_mhz:
+        clk = rates["sms"] * clock_mhz * 1e6
+        per_clk = {"ffma_lanes": rates["ffma"] / clk, "ffma2_lanes": rates["ffma2"] / clk,
+                   "ex2": rates["ex2"] / clk, "rsqrt": rates["rsqrt"] / clk}
+    return {"bound": bound, "achieved": achieved, "peak": peak, "frac": achieved / peak,
+            "pipe_frac": fr, "ops_per_unit": {"fp32": ops[0], "ex2": ops[1], "rsqrt": ops[2]},
+            "pipe_rates_lane_ops_per_s": {k: rates[k] for k in ("ffma", "ffma2", "ex2", "rsqrt")},
+            "pipe_rates_per_sm_clk": per_clk}
 
 
 # ---------------------------------------------------------------------------
@@ -183,47 +259,107 @@ class ClockSampler:
 # ---------------------------------------------------------------------------
 # CPU baseline: the FP64 treecode restatement on the host cores
 # ---------------------------------------------------------------------------
-def cpu_treecode_sample(wl, target_seconds, threads, leaf=None):
-    """Build the CPU plan (timed), convolve a sample of whole target batches
-    sized to ~target_seconds of field work, extrapolate to one convolution by
-    the pair counts of the full lists.  Returns (seconds per convolution, info)."""
-    from oracle import oracle as O
-    O.build()
-    mesh = wl["mesh"]
-    sl, tl = leaf or LEAF["hartree"]
-    t0 = time.perf_counter()
-    plan = O.Plan(mesh.x, mesh.y, mesh.z, mesh.x, mesh.y, mesh.z, mesh.w, THETA, DEGREE, sl, tl, 1.0)
-    t_plan = time.perf_counter() - t0
+def batch_pairs(plan):
+    """Pair count of every target batch of an oracle plan (near + far)."""
     L = plan.lists()
     st, tt = plan.tree(0), plan.tree(1)
-    nb = plan.n_batches
-    bsz = tt["end"][L["batch_node"]] - tt["begin"][L["batch_node"]]
-    ncnt = np.zeros(nb)
-    src_len = st["end"] - st["begin"]
-    for b in range(nb):
-        ncnt[b] = src_len[L["near_list"][L["near_off"][b]:L["near_off"][b + 1]]].sum()
-    pairs_b = bsz * (ncnt + np.diff(L["far_off"]) * plan.P)
-    total_pairs = pairs_b.sum()
-    rng = np.random.default_rng(17)
-    order = rng.permutation(nb)
-    q = wl["values"][0]
-    kp = wl["kparams"][0]
-    # calibration on a few batches, then a sample sized to the time target
-    sel = np.sort(order[:4])
-    _, (t_up, t_f), (pn, pf) = O.convolve_batches(plan, q, q, mesh.w, wl["kernel"], kp,
-                                                  wl["singularity"], sel, threads)
-    rate = (pn + pf) / max(t_f, 1e-9)
-    want = rate * target_seconds
-    csum = np.cumsum(pairs_b[order])
-    nsel = int(np.clip(np.searchsorted(csum, want) + 1, 4, nb))
-    sel = np.sort(order[:nsel])
-    _, (t_up, t_f), (pn, pf) = O.convolve_batches(plan, q, q, mesh.w, wl["kernel"], kp,
-                                                  wl["singularity"], sel, threads)
-    frac = (pn + pf) / total_pairs
-    seconds = t_plan + t_up + t_f / frac
-    return seconds, dict(batches=int(nsel), of_batches=int(nb), pair_fraction=float(frac),
-                         plan_s=t_plan, upward_s=t_up, sample_field_s=t_f,
-                         pairs_per_s=(pn + pf) / t_f, total_pairs=float(total_pairs))
+    bn = L["batch_node"]
+    bsz = (tt["end"][bn] - tt["begin"][bn]).astype(np.float64)
+    src_len = (st["end"] - st["begin"]).astype(np.float64)
+    cs = np.concatenate([[0.0], np.cumsum(src_len[L["near_list"]])])
+    near = cs[L["near_off"][1:]] - cs[L["near_off"][:-1]]
+    return bsz * (near + np.diff(L["far_off"]) * plan.P)
+
+
+def stratified_batches(pairs_b, count):
+    """`count` batches evenly spread over the batches sorted by pair count
+    (lightest and heaviest included): a fixed, deterministic sample."""
+    order = np.argsort(pairs_b, kind="stable")
+    pick = np.unique(np.linspace(0, len(order) - 1, min(count, len(order))).round().astype(int))
+    return np.sort(order[pick])
+
+
+class CpuTreecode:
+    """The oracle's FP64 treecode for one workload: the plan (timed once),
+    a fixed stratified sample of target batches, and per-orbital samples
+    extrapolated by pair count.  Both the reference arm and the GPU arm's
+    cpu_baseline leg use this, so they time the same thing."""
+
+    def __init__(self, wl, threads, leaf=None, nbatches=CPU_SAMPLE_BATCHES):
+        from oracle import oracle as O
+        O.build()
+        self.O, self.wl, self.threads = O, wl, threads
+        mesh = wl["mesh"]
+        sl, tl = leaf or LEAF["hartree"]
+        t0 = time.perf_counter()
+        self.plan = O.Plan(mesh.x, mesh.y, mesh.z, mesh.x, mesh.y, mesh.z, mesh.w, THETA, DEGREE, sl, tl, 1.0)
+        self.plan_s = time.perf_counter() - t0
+        self.pairs_b = batch_pairs(self.plan)
+        self.total_pairs = float(self.pairs_b.sum())
+        self.sel = stratified_batches(self.pairs_b, nbatches)
+        self.halves = (self.sel[0::2], self.sel[1::2])
+
+    def orbital(self, o):
+        """Seconds of one orbital's convolution (upward pass in full, fields
+        extrapolated from the two halves of the sample) and the two halves'
+        own estimates (their difference is the sample's spread)."""
+        O, wl, mesh = self.O, self.wl, self.wl["mesh"]
+        q = wl["values"][o]
+        kp = wl["kparams"][o]
+        est, t_f, frac, t_up = [], 0.0, 0.0, 0.0
+        for half in self.halves:
+            _, (tu, tf), (pn, pf) = O.convolve_batches(self.plan, q, q, mesh.w, wl["kernel"], kp,
+                                                       wl["singularity"], half, self.threads)
+            fr = (pn + pf) / self.total_pairs
+            est.append(tu + tf / fr)
+            t_f += tf
+            frac += fr
+            t_up = tu
+        return t_up + t_f / frac, est, dict(upward_s=t_up, sample_field_s=t_f, pair_fraction=frac,
+                                            pairs_per_s=frac * self.total_pairs / t_f)
+
+    def gram_schmidt_seconds(self, norb):
+        """The oracle's FP64 Gram-Schmidt (Orthogonalization.c:14-119 restated)
+        over norb orbitals of the mesh, in full, single-threaded."""
+        n = self.wl["mesh"].n
+        rng = np.random.default_rng(5)
+        V = rng.standard_normal((norb, n))
+        t0 = time.perf_counter()
+        for j in range(norb):
+            self.O.mgs(V, V[j].copy(), self.wl["mesh"].w, j)
+        return time.perf_counter() - t0
+
+
+def cpu_step_estimate(cpu, norb, orbitals, mgs_s):
+    """Seconds of one full step (plan + norb orbital convolutions [+ MGS]) from
+    the orbitals sampled; returns (seconds, spread, info)."""
+    per, halves, infos = [], [], []
+    for o in orbitals:
+        s, est, info = cpu.orbital(o)
+        per.append(s)
+        halves.append(est)
+        infos.append(info)
+    mean = float(np.mean(per))
+    seconds = cpu.plan_s + norb * mean + mgs_s
+    h = np.array(halves)
+    alt = [cpu.plan_s + norb * float(np.mean(h[:, i])) + mgs_s for i in range(2)]
+    spread = abs(alt[0] - alt[1]) / seconds
+    return seconds, spread, dict(orbital_s=per, half_estimates_s=alt, plan_s=cpu.plan_s, gram_schmidt_s=mgs_s,
+                                 pair_fraction=infos[0]["pair_fraction"], pairs_per_s=infos[0]["pairs_per_s"],
+                                 batches=int(len(cpu.sel)), of_batches=int(len(cpu.pairs_b)))
+
+
+def cpu_anchor(threads):
+    """One whole FP64 convolution by the oracle, unsampled: the single Z = 4
+    atom, 50,112 points, leaves 500, Yukawa k = 1 with subtraction."""
+    from oracle import oracle as O
+    pkg = importlib.import_module(PKG)
+    BT = pkg.BaryTreeInterface
+    mesh, f, rho = pkg.synthetic.single_atom(factor=1.0, max_depth=5)
+    t0 = time.perf_counter()
+    plan = O.Plan(mesh.x, mesh.y, mesh.z, mesh.x, mesh.y, mesh.z, mesh.w, THETA, DEGREE, PLAIN_LEAF, PLAIN_LEAF, 1.0)
+    out = plan.convolve(f, f, mesh.w, BT.Kernel.YUKAWA, [1.0], BT.Singularity.SUBTRACTION, nthreads=threads)
+    return time.perf_counter() - t0, mesh, f, out
 
 
 def reference_arm_mesh(args):
@@ -289,57 +425,57 @@ def reference_arm(args):
                 "data": "synthetic ring molecule (seeded)", **body}
         print(json.dumps(line), flush=True)
         return 0
-    if args.workload == "scf":
-        print(json.dumps({"impl": "reference", "unavailable": "the reference SCF needs its atomic data files "
-                          "and BaryTree, neither of which is present"}), flush=True)
+    if args.workload in ("scf", "uneven"):
+        why = ("the reference SCF needs its atomic data files and BaryTree, neither of which is present"
+               if args.workload == "scf" else
+               "the reference has no multi-system call; its per-orbital CPU cost is the orbitals workload's line")
+        print(json.dumps({"impl": "reference", "unavailable": why}), flush=True)
         return 0
     wl = make_workload(args.workload)
+    norb = int(wl["values"].shape[0])
     threads = os.cpu_count() or 1
-    per_step = max(2.0, args.cpu_seconds / 4)
-    for _ in range(args.warmup):
-        cpu_treecode_sample(wl, per_step, threads)
-    secs, info = [], None
     t0 = time.perf_counter()
-    for _ in range(args.steps):
-        s, info = cpu_treecode_sample(wl, per_step, threads)
-        secs.append(s)
-    wall = time.perf_counter() - t0
+    cpu = CpuTreecode(wl, threads)
+    mgs_s = cpu.gram_schmidt_seconds(norb) if wl["mgs"] else 0.0
+    setup_s = time.perf_counter() - t0
+    secs, walls, spreads, info = [], [], [], None
+    for k in range(args.warmup + args.steps):
+        a = time.perf_counter()
+        s, spread, info = cpu_step_estimate(cpu, norb, [k % norb], mgs_s)
+        if k >= args.warmup:
+            secs.append(s)
+            spreads.append(spread)
+            walls.append(time.perf_counter() - a)
     mean_s = float(np.mean(secs))
-    value = 1.0 / mean_s
-    sample = (f"FP64 treecode restatement (oracle/tagi_oracle.c, OpenMP) on {info['batches']} of "
-              f"{info['of_batches']} target batches per step ({info['pair_fraction']:.4f} of the "
-              "pairs), plan + upward pass timed in full, fields extrapolated by pair count")
+    value = norb / mean_s
+    sample = (f"FP64 treecode restatement (oracle/tagi_oracle.c, OpenMP, {threads} threads): plan built and timed "
+              f"once ({cpu.plan_s:.2f} s); per step one orbital (orbital = step index mod {norb}): upward pass "
+              f"in full, fields on a fixed stratified sample of {info['batches']} of {info['of_batches']} target "
+              f"batches ({info['pair_fraction']:.4f} of the pairs), extrapolated by pair count to {norb} orbitals"
+              + (f"; plus the FP64 Gram-Schmidt of the {norb} orbitals timed in full once ({mgs_s:.2f} s)"
+                 if wl["mgs"] else ""))
     line = {"impl": "reference", "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": 0,
-            "steps": args.steps, "warmup": args.warmup, "ms_per_step": mean_s * 1e3,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": float(np.mean(walls)) * 1e3,
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
             "data": "synthetic (seeded)",
-            "config": {"workload": wl["desc"], "points": int(wl["mesh"].n), "theta": THETA,
-                       "degree": DEGREE, "leaf": list(LEAF["hartree"]), "precision": "fp64"},
-            "cpu_baseline": {"value": value, "unit": UNIT, "cores": threads, "kind": "port",
-                             "sample": sample},
+            "config": {"workload": wl["desc"], "points": int(wl["mesh"].n), "orbitals": norb, "theta": THETA,
+                       "degree": DEGREE, "leaf": list(LEAF[args.workload]), "precision": "fp64"},
+            "cpu_baseline": {"value": value, "unit": UNIT, "cores": threads, "kind": "port", "sample": sample,
+                             "spread": float(np.max(spreads)),
+                             "spread_note": "largest relative difference between the estimates from the two "
+                                            "halves of the sample"},
             "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
-            "wall_s": wall, "cpu_pairs_per_s": info["pairs_per_s"]}
+            "ms_per_step_note": "measured wall time of one sample step; the full step it stands for is "
+                                "extrapolated_ms_per_full_step",
+            "extrapolated_ms_per_full_step": mean_s * 1e3, "setup_s": setup_s,
+            "cpu_pairs_per_s": info["pairs_per_s"]}
     print(json.dumps(line), flush=True)
     return 0
 
 
 # ---------------------------------------------------------------------------
-# GB300 arm
+# GB300 arm: one convolution call (Hartree) or the 32-orbital batch + Gram-Schmidt
 # ---------------------------------------------------------------------------
-def profile_traffic(kernel, label):
-    """DRAM bytes per launch of a field kernel from the committed ncu summary."""
-    path = os.path.join(ROOT, "profiles", f"{kernel}_field_{label}_1.5M.md")
-    if not os.path.exists(path):
-        return None
-    for line in open(path):
-        if line.startswith("dram_bytes_per_launch"):
-            try:
-                return float(line.split("=")[1].split()[0])
-            except (IndexError, ValueError):
-                return None
-    return None
-
-
 def gb300_arm(args):
     import torch
     import torch.distributed as dist
@@ -350,29 +486,35 @@ def gb300_arm(args):
         dist.init_process_group("nccl", device_id=torch.device("cuda", local))
     pkg = importlib.import_module(PKG)
     dev = importlib.import_module(PKG + ".device")
+    gi = importlib.import_module(PKG + ".gi")
     nat = pkg._native
     L = nat.lib()
     wl = make_workload(args.workload)
     mesh = wl["mesh"]
+    K, SS = wl["kernel"], wl["singularity"]
     cuda = torch.device("cuda", local)
     t = lambda a: torch.as_tensor(np.ascontiguousarray(a), dtype=torch.float64, device=cuda)
     x, y, z, w = t(mesh.x), t(mesh.y), t(mesh.z), t(mesh.w)
     vals = t(wl["values"])
     norb = vals.shape[0]
+    kp = wl["kparams"]
     sl, tl = LEAF[args.workload]
     stream = torch.cuda.current_stream()
+    V = torch.empty_like(vals)
+    mgs = wl["mgs"]
 
-    def step():
-        plan = dev.TreecodePlan.for_mesh(x, y, z, w, theta=THETA, degree=DEGREE, source_leaf=sl,
-                                         target_leaf=tl)
-        out = plan.convolve(vals, vals, wl["kernel"], wl["kparams"], wl["singularity"],
-                            precision="mixed")
+    def step(gram_schmidt=True):
+        plan = dev.TreecodePlan.for_mesh(x, y, z, w, theta=THETA, degree=DEGREE, source_leaf=sl, target_leaf=tl)
+        plan.convolve(vals, vals, K, kp, SS, precision="mixed", out=V)
         info = plan.info()
         plan.close()
-        return out, info
+        # psi' = conv / 4 pi, orthonormalized: the constant factor drops out of Gram-Schmidt
+        if mgs and gram_schmidt:
+            gi.orthonormalize(V, w, stream)
+        return info
 
     for _ in range(args.warmup):
-        out, info = step()
+        info = step()
     torch.cuda.synchronize()
     flush = torch.empty(64 * 1024 * 1024, dtype=torch.float32, device=cuda)  # 256 MB > L2
     evs = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True))
@@ -390,7 +532,7 @@ def gb300_arm(args):
         for k in range(args.steps):
             flush.zero_()
             evs[k][0].record(stream)
-            out, info = step()
+            info = step()
             evs[k][1].record(stream)
         torch.cuda.synchronize()
         if ws > 1:
@@ -398,6 +540,7 @@ def gb300_arm(args):
         launches = L.tagi_launch_count() - n0
     L.tagi_profile_read(nat.dptr(prof_ms), prof_np, 7)
     L.tagi_profile(0)
+    clk = clocks.summary()
     step_ms = [a.elapsed_time(b) for a, b in evs]
     total_ms = job_time_ms(float(sum(step_ms)), cuda)
     value = job_value(norb, args.steps, ws, total_ms)
@@ -407,94 +550,177 @@ def gb300_arm(args):
             dist.destroy_process_group()
         return 0
 
-    # accuracy of the timed result against the exact FP64 direct sum (GPU) on seeded targets
-    rng = np.random.default_rng(99)
-    sub = torch.as_tensor(np.sort(rng.choice(mesh.n, 4096, replace=False)).astype(np.int32),
-                          device=cuda)
-    o0 = out[0].contiguous()
-    ref = dev.direct(x, y, z, vals[0].contiguous(), x, y, z, vals[0].contiguous(), w, wl["kernel"],
-                     wl["kparams"][0], wl["singularity"], subset=sub)
-    rel = float(torch.linalg.norm(o0[sub.long()] - ref) / torch.linalg.norm(ref))
-
-    # roofline of the dominant field kernel
-    # the ordinary near pass processes the near pairs outside close ranges
-    pairs_near = (info["near_pairs"] - info["near_close_pairs"]) * norb
-    pairs_far = info["far_pairs"] * norb
-    near_ms = prof_ms[3] / max(prof_n[3], 1)
-    far_ms = prof_ms[4] / max(prof_n[4], 1)
-    dominant = "near" if near_ms >= far_ms else "far"
-    k_ms = near_ms if dominant == "near" else far_ms
-    k_pairs = pairs_near if dominant == "near" else pairs_far
-    achieved = k_pairs / (k_ms * 1e-3)
-    peak = ctypes.c_double()
-    kp0 = float(wl["kparams"][0][0])
-    nat.check(L.tagi_pair_peak(int(wl["kernel"]), int(wl["singularity"]),
-                               0 if dominant == "near" else 1, kp0, ctypes.byref(peak),
-                               ctypes.c_void_p(stream.cuda_stream)))
-    traffic = profile_traffic(dominant, wl["label"])
-    roofline = {"bound": "mufu", "achieved": achieved / 1e9, "peak": peak.value / 1e9,
-                "unit": "Gpair/s", "frac": achieved / peak.value, "traffic": traffic,
-                "kernel": f"{dominant}_mixed ({wl['label']})",
-                "peak_source": "tagi_pair_peak: same pair arithmetic, operands in shared "
-                               "memory/registers, measured live on this GPU",
-                "kernel_ms_per_launch": k_ms, "pairs_per_launch": k_pairs,
-                "fp32_tflops": achieved * PAIR_FLOPS[wl["label"]] / 1e12}
-
-    # end to end through the C ABI with pinned host buffers
-    pinned = [torch.empty(mesh.n, dtype=torch.float64, pin_memory=True) for _ in range(9)]
-    for p_, a_ in zip(pinned, (mesh.x, mesh.y, mesh.z, wl["values"][0], mesh.x, mesh.y, mesh.z,
-                               wl["values"][0], mesh.w)):
-        p_.numpy()[:] = a_
-    hout = torch.empty(mesh.n, dtype=torch.float64, pin_memory=True)
-    hp = [nat.dptr(p_.numpy()) for p_ in pinned]
-    kpar = np.ascontiguousarray(wl["kparams"][0], dtype=np.float64)
-
-    def e2e_call():
-        return L.tagi_BaryTreeInterface_ex(mesh.n, mesh.n, *hp, nat.dptr(hout.numpy()),
-                                           int(wl["kernel"]), len(kpar), nat.dptr(kpar),
-                                           int(wl["singularity"]), 1, 1, THETA, DEGREE, sl, tl,
-                                           1.0, -1.0, 0, nat.PREC_MIXED)
-    nat.check(e2e_call())
-    e2e_steps = max(1, min(args.steps, 3))
+    # Gram-Schmidt alone and the convolution alone (untimed for the headline)
+    ev = [torch.cuda.Event(enable_timing=True) for _ in range(4)]
+    ev[0].record(stream)
+    step(gram_schmidt=False)
+    ev[1].record(stream)
+    if mgs:
+        gi.orthonormalize(V, w, stream)
+    ev[2].record(stream)
     torch.cuda.synchronize()
-    t0 = time.perf_counter()
+    conv_ms, mgs_ms = ev[0].elapsed_time(ev[1]), ev[1].elapsed_time(ev[2])
+
+    # accuracy of the convolution against the exact FP64 direct sum (GPU, tested against the oracle)
+    plan = dev.TreecodePlan.for_mesh(x, y, z, w, theta=THETA, degree=DEGREE, source_leaf=sl, target_leaf=tl)
+    out = plan.convolve(vals, vals, K, kp, SS, precision="mixed")
+    plan.close()
+    rng = np.random.default_rng(99)
+    sub = torch.as_tensor(np.sort(rng.choice(mesh.n, 4096, replace=False)).astype(np.int32), device=cuda)
+    errs = {}
+    for o in sorted({0, norb - 1}):
+        vo = vals[o].contiguous()
+        ref = dev.direct(x, y, z, vo, x, y, z, vo, w, K, kp[o], SS, subset=sub)
+        errs[int(o)] = float(torch.linalg.norm(out[o][sub.long()] - ref) / torch.linalg.norm(ref))
+    del out
+
+    # roofline: the dominant field kernel against the hardware pipes
+    og = 8 if (norb >= 8 and wl["label"].startswith("yukawa")) else (4 if norb >= 4 and wl["label"].startswith("yukawa") else 1)
+    names = ("near_group", "far_group") if og > 1 else ("near_mixed", "far_mixed")
+    units = {names[0]: (info["near_pairs"] - info["near_close_pairs"]) * norb, names[1]: info["far_pairs"] * norb}
+    kms = {names[0]: prof_ms[3] / max(prof_n[3], 1), names[1]: prof_ms[4] / max(prof_n[4], 1)}
+    rates = pipe_rates(L, nat, stream)
+    roofs = {}
+    for kname in names:
+        r = pipe_roofline(units[kname], kms[kname], field_ops(kname, wl["label"], og, DEGREE + 1), rates,
+                          clk.get("sm_mhz"))
+        variant = {"near_mixed": 0, "far_mixed": 1, "near_group": 2, "far_group": 3}[kname]
+        lp = ctypes.c_double()
+        nat.check(L.tagi_pair_peak(int(K), int(SS), variant, float(kp[0][0]), ctypes.byref(lp),
+                                   ctypes.c_void_p(stream.cuda_stream)))
+        r.update({"kernel": f"{kname} ({wl['label']}" + (f", {og} orbitals per item)" if og > 1 else ")"),
+                  "kernel_ms_per_launch": kms[kname], "units_per_launch": units[kname],
+                  "unit": "Gpair-orbitals/s" if og > 1 else "Gpair/s",
+                  "loop_peak": lp.value / 1e9, "loop_efficiency": units[kname] / (kms[kname] * 1e-3) / lp.value})
+        r["achieved"] /= 1e9
+        r["peak"] /= 1e9
+        roofs[kname] = r
+    dom = names[0] if kms[names[0]] >= kms[names[1]] else names[1]
+    roofline = dict(roofs[dom], traffic=None,
+                    traffic_note="DRAM bytes per launch are in the committed ncu summary of this kernel "
+                                 "(profiles/); the pairwise sums read each source tile from L2")
+    roofline["peak_source"] = ("hardware pipe rates measured live on this GPU (tagi_pipe_rates: FFMA lanes, MUFU "
+                               "ex2, MUFU rsqrt, every SM busy, no memory traffic) and the kernel's per-unit "
+                               "operation counts")
+
+    # end to end from pinned host memory through the public one-shot call
+    if mgs:
+        hx, hy, hz, hw = (torch.as_tensor(getattr(mesh, a)).pin_memory() for a in "xyzw")
+        hv = torch.as_tensor(np.ascontiguousarray(wl["values"])).pin_memory()
+        hout = torch.empty_like(hv).pin_memory()
+        off = np.array([0, mesh.n], dtype=np.int32)
+        kall = np.ascontiguousarray(kp[:, 0])
+
+        def e2e_call():
+            dx, dy, dz, dw, dv = (h.to(cuda, non_blocking=True) for h in (hx, hy, hz, hw, hv))
+            o = dev.treecode_batched(off, [norb], dx, dy, dz, dw, dv, K, kall, SS, theta=THETA, degree=DEGREE,
+                                     source_leaf=sl, target_leaf=tl, precision="mixed")
+            gi.orthonormalize(o, dw, stream)
+            hout.copy_(o, non_blocking=True)
+        h2d = 8 * (4 * mesh.n + hv.numel())
+        d2h = 8 * hout.numel()
+        path = "tagi_treecode_batched (one-shot: plan built inside the call) + Gram-Schmidt, pinned host buffers"
+    else:
+        pinned = [torch.empty(mesh.n, dtype=torch.float64, pin_memory=True) for _ in range(9)]
+        for p_, a_ in zip(pinned, (mesh.x, mesh.y, mesh.z, wl["values"][0], mesh.x, mesh.y, mesh.z,
+                                   wl["values"][0], mesh.w)):
+            p_.numpy()[:] = a_
+        hout = torch.empty(mesh.n, dtype=torch.float64, pin_memory=True)
+        hp = [nat.dptr(p_.numpy()) for p_ in pinned]
+        kpar = np.ascontiguousarray(kp[0], dtype=np.float64)
+
+        def e2e_call():
+            nat.check(L.tagi_BaryTreeInterface_ex(mesh.n, mesh.n, *hp, nat.dptr(hout.numpy()), int(K), len(kpar),
+                                                  nat.dptr(kpar), int(SS), 1, 1, THETA, DEGREE, sl, tl, 1.0, -1.0,
+                                                  0, nat.PREC_MIXED))
+        h2d, d2h = 9 * 8 * mesh.n, 8 * mesh.n
+        path = "tagi_BaryTreeInterface_ex (the C ABI BaryTreeInterface binds, host buffers)"
+    e2e_call()
+    torch.cuda.synchronize()
+    e2e_steps = max(1, min(args.steps, 3))
+    e2e_s = []
     for _ in range(e2e_steps):
         flush.zero_()
         torch.cuda.synchronize()
-        nat.check(e2e_call())
-    e2e_s = (time.perf_counter() - t0) / e2e_steps
-    e2e = {"value": 1.0 / e2e_s, "unit": UNIT, "h2d_bytes_per_step": 9 * 8 * mesh.n,
-           "d2h_bytes_per_step": 8 * mesh.n, "path": "tagi_BaryTreeInterface_ex (C ABI, host buffers)",
-           "note": "per step one single-charge-vector call"}
+        a = time.perf_counter()
+        e2e_call()
+        torch.cuda.synchronize()
+        e2e_s.append(time.perf_counter() - a)
+    e2e = {"value": norb / float(np.mean(e2e_s)), "unit": UNIT, "h2d_bytes_per_step": int(h2d),
+           "d2h_bytes_per_step": int(d2h), "path": path}
+
+    # the plain FP64 path: one tagi_treecode_dev call per orbital (tree + convolution), leaves 500
+    vs_plain = None
+    if not args.no_plain and mgs:
+        plain = {}
+        for o in sorted({0, norb - 1}):
+            vo = vals[o].contiguous()
+            torch.cuda.synchronize()
+            a = time.perf_counter()
+            dev.treecode(x, y, z, vo, x, y, z, vo, w, K, kp[o], SS, THETA, DEGREE, PLAIN_LEAF, PLAIN_LEAF,
+                         precision="fp64")
+            torch.cuda.synchronize()
+            plain[int(o)] = time.perf_counter() - a
+        plain_rate = 1.0 / float(np.mean(list(plain.values())))
+        conv_rate = norb / (conv_ms * 1e-3)
+        vs_plain = {"plain_fp64_orbital_convs_per_s": plain_rate, "seconds_per_orbital": plain,
+                    "batched_mixed_orbital_convs_per_s": conv_rate, "speedup": conv_rate / plain_rate,
+                    "note": "plain: one FP64 tagi_treecode_dev call per orbital (tree + convolution, leaves "
+                            f"{PLAIN_LEAF}), orbitals timed as listed; batched: plan + the {norb}-orbital "
+                            "mixed-precision convolution (no Gram-Schmidt), CUDA events"}
 
     cpu = None
     if not args.no_cpu_baseline and ws == 1:
         threads = os.cpu_count() or 1
-        secs, cinfo = cpu_treecode_sample(wl, args.cpu_seconds, threads)
-        cpu = {"value": norb / secs if args.workload == "hartree" else 1.0 / secs, "unit": UNIT,
-               "cores": threads, "kind": "port",
-               "sample": (f"FP64 treecode restatement on {cinfo['batches']} of {cinfo['of_batches']} "
-                          f"target batches ({cinfo['pair_fraction']:.4f} of the pairs), plan and "
-                          "upward pass timed in full, fields extrapolated by pair count")}
+        c = CpuTreecode(wl, threads)
+        mgs_s = c.gram_schmidt_seconds(norb) if mgs else 0.0
+        secs, spread, cinfo = cpu_step_estimate(c, norb, [0], mgs_s)
+        a_s, amesh, af, aout = cpu_anchor(threads)
+        ax, ay, az, aw, aft = (t(v) for v in (amesh.x, amesh.y, amesh.z, amesh.w, af))
+        gpu_anchor = {}
+        for prec in ("fp64", "mixed"):
+            dev.treecode(ax, ay, az, aft, ax, ay, az, aft, aw, 2, [1.0], 2, THETA, DEGREE, PLAIN_LEAF, PLAIN_LEAF,
+                         precision=prec)
+            torch.cuda.synchronize()
+            a = time.perf_counter()
+            g = dev.treecode(ax, ay, az, aft, ax, ay, az, aft, aw, 2, [1.0], 2, THETA, DEGREE, PLAIN_LEAF,
+                             PLAIN_LEAF, precision=prec)
+            torch.cuda.synchronize()
+            gpu_anchor[prec] = {"seconds": time.perf_counter() - a,
+                                "rel_l2_vs_oracle": float(np.linalg.norm(g.cpu().numpy() - aout) / np.linalg.norm(aout))}
+        cpu = {"value": norb / secs, "unit": UNIT, "cores": threads, "kind": "port",
+               "sample": (f"FP64 treecode restatement (oracle/tagi_oracle.c, OpenMP): plan in full "
+                          f"({cinfo['plan_s']:.2f} s), orbital 0's upward pass in full and its fields on a fixed "
+                          f"stratified sample of {cinfo['batches']} of {cinfo['of_batches']} target batches "
+                          f"({cinfo['pair_fraction']:.4f} of the pairs), extrapolated by pair count to {norb} "
+                          "orbitals" + (f", plus the FP64 Gram-Schmidt of {norb} orbitals in full "
+                                        f"({mgs_s:.2f} s, one thread)" if mgs else "")),
+               "spread": spread,
+               "anchor": {"what": "one whole FP64 convolution, unsampled: single Z = 4 atom, 50,112 points, "
+                                  "leaves 500, Yukawa k = 1 with subtraction",
+                          "cpu_seconds": a_s, "gpu": gpu_anchor}}
 
-    clk = clocks.summary()
     line = {
         "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": ws, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": total_ms / args.steps, "higher_is_better": True,
         "scaling": "weak", "vs_baseline": None, "dtype": "f32+f64",
-        "data": "synthetic (seeded mesh and densities)",
+        "data": "synthetic (seeded mesh and orbitals)",
         "config": {"workload": wl["desc"], "points": int(mesh.n), "orbitals": int(norb),
                    "theta": THETA, "degree": DEGREE, "leaf": [sl, tl], "precision": "mixed",
-                   "step": "plan (tree, lists, weight charges) + convolution, inputs in HBM",
+                   "step": ("plan (tree, lists, weight charges) + one batched convolution of all orbitals"
+                            + (" + FP64 Gram-Schmidt of the results" if mgs else "") + ", inputs in HBM"),
                    "l2": "256 MB buffer written between timed steps (untimed)",
                    "parallelism": f"replicas x{ws} (independent convolutions, no collective)",
-                   "rel_l2_vs_fp64_direct": rel, "rel_l2_sample_targets": 4096,
+                   "rel_l2_vs_fp64_direct": max(errs.values()), "rel_l2_by_orbital": errs,
+                   "rel_l2_sample_targets": 4096,
                    "pairs_per_conv": info["near_pairs"] + info["far_pairs"],
                    "near_pairs": info["near_pairs"], "far_pairs": info["far_pairs"],
                    "near_close_pairs": info["near_close_pairs"]},
         "phase_ms_per_step": {k: float(v) / args.steps for k, v in zip(
             ("tree", "lists", "upward", "near", "far", "glue", "near_close"), prof_ms)},
-        "roofline": roofline, "cpu_baseline": cpu, "e2e": e2e, "clocks": clk,
+        "convolution_ms": conv_ms, "gram_schmidt_ms": mgs_ms if mgs else None,
+        "roofline": roofline, "roofline_other": roofs[names[1] if dom == names[0] else names[0]],
+        "vs_plain": vs_plain, "cpu_baseline": cpu, "e2e": e2e, "clocks": clk,
         "gpu_launches": int(launches),
     }
     print(json.dumps(line), flush=True)
@@ -507,7 +733,6 @@ def gb300_arm(args):
 # Uneven multi-system batch: one persistent launch per pass, CUDA graph
 # ---------------------------------------------------------------------------
 UNEVEN_LEAVES = ((1000, 1000), (2000, 1000), (2000, 2000), (4000, 2000))
-PLAIN_LEAF = 500  # 500-point leaves, the tree parameters the reference's single-atom runs use
 
 
 def uneven_arm(args):
@@ -612,17 +837,28 @@ def uneven_arm(args):
     pairs_all = sum((i["near_pairs"] + i["far_pairs"]) * no for i, no in zip(infos, norbs))
     near_ms, far_ms = prof_ms[3], prof_ms[4]
     og = S.info()["orbitals_per_item"]
-    peak = ctypes.c_double()
-    nat.check(L.tagi_pair_peak(int(K), int(SS), 2 if og > 1 else 0, 1.0, ctypes.byref(peak),
-                               ctypes.c_void_p(torch.cuda.current_stream().cuda_stream)))
-    achieved = pairs_near / (near_ms * 1e-3)
-    roofline = {"bound": "mufu", "achieved": achieved / 1e9, "peak": peak.value / 1e9, "unit": "Gpair/s",
-                "frac": achieved / peak.value, "traffic": None,
-                "kernel": f"near_group<OG={og}> over all systems" if og > 1 else "near_mixed over all systems",
-                "peak_source": "tagi_pair_peak variant 2 (orbital-group near loop, 8 orbitals per pair "
-                               "geometry), measured live on this GPU" if og > 1 else "tagi_pair_peak variant 0",
-                "kernel_ms_per_launch": near_ms, "pairs_per_launch": pairs_near,
-                "far_ms_per_launch": far_ms, "far_pairs_per_launch": pairs_far}
+    stream0 = torch.cuda.current_stream()
+    rates = pipe_rates(L, nat, stream0)
+    n1max = DEGREE + 1
+    names = ("near_group", "far_group") if og > 1 else ("near_mixed", "far_mixed")
+    roofs = {}
+    for kname, units, kms in ((names[0], pairs_near, near_ms), (names[1], pairs_far, far_ms)):
+        r = pipe_roofline(units, kms, field_ops(kname, "yukawa_ss", og, n1max), rates, None)
+        lp = ctypes.c_double()
+        variant = {"near_mixed": 0, "far_mixed": 1, "near_group": 2, "far_group": 3}[kname]
+        nat.check(L.tagi_pair_peak(int(K), int(SS), variant, 1.0, ctypes.byref(lp),
+                                   ctypes.c_void_p(stream0.cuda_stream)))
+        r.update({"kernel": f"{kname} over all systems" + (f" ({og} orbitals per item)" if og > 1 else ""),
+                  "kernel_ms_per_launch": kms, "units_per_launch": units,
+                  "unit": "Gpair-orbitals/s" if og > 1 else "Gpair/s", "loop_peak": lp.value / 1e9,
+                  "loop_efficiency": units / (kms * 1e-3) / lp.value})
+        r["achieved"] /= 1e9
+        r["peak"] /= 1e9
+        roofs[kname] = r
+    dom = names[0] if near_ms >= far_ms else names[1]
+    roofline = dict(roofs[dom], traffic=None,
+                    peak_source="hardware pipe rates measured live (tagi_pipe_rates) and the kernel's per-unit "
+                                "operation counts")
 
     # plain path: one FP64 tagi_treecode_dev call per orbital (tree + convolution), leaves 500
     plain = []
@@ -671,15 +907,16 @@ def uneven_arm(args):
     cpu = None
     if not args.no_cpu_baseline and ws == 1:
         threads = os.cpu_count() or 1
-        i = 2  # 300k-point system: CPU FP64 pair rate on a sample of its batches
+        i = 2  # 300k-point system: CPU FP64 pair rate on a stratified sample of its batches
         m, F, k = systems[i]
-        wl = dict(mesh=m, values=F, kparams=k[:, None], kernel=K, singularity=SS)
-        secs, cinfo = cpu_treecode_sample(wl, args.cpu_seconds, threads, leaf=tuned["leaves"][i])
+        wl = dict(mesh=m, values=F, kparams=k[:, None], kernel=K, singularity=SS, mgs=False)
+        c = CpuTreecode(wl, threads, leaf=tuned["leaves"][i])
+        _, _, cinfo = cpu_step_estimate(c, 1, [0], 0.0)
         rate = cinfo["pairs_per_s"]
         cpu_s = sum(no * (i_["near_pairs"] + i_["far_pairs"]) / rate for i_, no in zip(infos, norbs))
         cpu = {"value": orb_total / cpu_s, "unit": "orbital convolutions/s", "cores": threads, "kind": "port",
-               "sample": (f"FP64 treecode restatement on {cinfo['batches']} of {cinfo['of_batches']} batches "
-                          f"of the {m.n}-point system (one orbital); its pair rate "
+               "sample": (f"FP64 treecode restatement on a stratified {cinfo['batches']} of {cinfo['of_batches']} "
+                          f"batches of the {m.n}-point system (one orbital); its pair rate "
                           f"{rate:.3g}/s applied to all {orb_total} orbital convolutions' pair counts")}
 
     clk = clocks.summary()
@@ -704,7 +941,8 @@ def uneven_arm(args):
             "measured_systems": len(plain), "seconds_per_orbital_measured": plain,
             "fp64_pairs_per_s": rate64, "speedup_of_batched": value / plain_value,
             "note": "systems beyond the measured ones extrapolated by their plain-tree pair counts"},
-        "roofline": roofline, "cpu_baseline": cpu, "e2e": e2e, "clocks": clk,
+        "roofline": roofline, "roofline_other": roofs[names[1] if dom == names[0] else names[0]],
+        "cpu_baseline": cpu, "e2e": e2e, "clocks": clk,
         "gpu_launches": launches_per_replay * args.steps,
     }
     print(json.dumps(line), flush=True)
@@ -1009,13 +1247,19 @@ def twomesh_arm(args):
     far_pairs = info["far_pairs"] * 22 * args.steps
     dominant = "near" if prof_ms[3] >= prof_ms[4] else "far"
     k_ms = prof_ms[3] if dominant == "near" else prof_ms[4]
-    k_pairs = near_pairs if dominant == "near" else far_pairs
-    peak = ctypes.c_double()
-    # 21 of the 22 orbital-convolutions per step run in one orbital-group
-    # launch (several orbitals per pair geometry): its near-loop peak is variant 2
-    nat.check(L.tagi_pair_peak(2, 2, 2 if dominant == "near" else 1, 1.0, ctypes.byref(peak),
-                               ctypes.c_void_p(torch.cuda.current_stream().cuda_stream)))
-    achieved = k_pairs / (k_ms * 1e-3)
+    # the phase holds two launches per step: the Hartree convolution (one
+    # orbital, near_mixed/far_mixed) and the 21 Yukawa orbitals (orbital
+    # groups of 8): its pipe-bound time is the sum of both launches' ops
+    rates = pipe_rates(L, nat, torch.cuda.current_stream())
+    n1 = DEGREE + 3
+    pairs1 = (near_pairs if dominant == "near" else far_pairs) / 22.0
+    mixes = ((pairs1, field_ops(f"{dominant}_mixed", "coulomb_ss", 1, n1)),
+             (21 * pairs1, field_ops(f"{dominant}_group", "yukawa_ss", 8, n1)))
+    fp32 = max(rates["ffma"], rates["ffma2"])
+    t_fma = sum(u * o[0] for u, o in mixes) / fp32
+    t_mufu = sum(u * (o[1] / rates["ex2"] + o[2] / rates["rsqrt"]) for u, o in mixes)
+    bound_ms = max(t_fma, t_mufu) * 1e3
+    achieved = (22 * pairs1) / (k_ms * 1e-3)
     # e2e: host orbitals and density in, corrected eigenvalues out
     e2e_ms = []
     for _ in range(args.steps):
@@ -1033,12 +1277,14 @@ def twomesh_arm(args):
                        "eigenvalue_corrections": [float(v) for v in out["deltaE"]]},
             "phase_ms_per_step": {k: float(prof_ms[i]) / args.steps for i, k in
                                   enumerate(("tree", "lists", "upward", "near", "far", "glue", "near_close"))},
-            "roofline": {"bound": "mufu", "kernel": f"{dominant}_mixed (yukawa/coulomb ss)",
-                         "achieved": achieved / 1e9, "peak": peak.value / 1e9, "unit": "Gpair/s",
-                         "frac": achieved / peak.value, "traffic": None,
-                         "peak_source": ("tagi_pair_peak variant 2 (orbital-group near loop, Yukawa SS), "
-                                         "measured live" if dominant == "near" else
-                                         "tagi_pair_peak variant 1 (far loop), measured live")},
+            "roofline": {"bound": "fp32" if t_fma >= t_mufu else "mufu",
+                         "kernel": f"{dominant} field: {dominant}_mixed (Hartree) + {dominant}_group (21 Yukawa "
+                                   "orbitals, groups of 8)",
+                         "achieved": achieved / 1e9, "peak": achieved / 1e9 * bound_ms / k_ms,
+                         "unit": "Gpair-orbitals/s", "frac": bound_ms / k_ms, "traffic": None,
+                         "pipe_frac": {"fp32": t_fma * 1e3 / k_ms, "mufu": t_mufu * 1e3 / k_ms},
+                         "peak_source": "hardware pipe rates measured live (tagi_pipe_rates) and the kernels' "
+                                        "per-unit operation counts"},
             "e2e": {"value": 21 / (statistics.median(e2e_ms) * 1e-3), "unit": "orbitals/s",
                     "h2d_bytes_per_step": int(psi.nbytes + rho.nbytes), "d2h_bytes_per_step": 8 * 21},
             "clocks": clocks.summary(), "gpu_launches": launches}
