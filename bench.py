@@ -260,7 +260,7 @@ class ClockSampler:
 # CPU baseline: the FP64 treecode restatement on the host cores
 # ---------------------------------------------------------------------------
 def batch_pairs(plan):
-    """Pair count of every target batch of an oracle plan (near + far)."""
+    """Near and far pair counts of every target batch of an oracle plan."""
     L = plan.lists()
     st, tt = plan.tree(0), plan.tree(1)
     bn = L["batch_node"]
@@ -268,7 +268,18 @@ def batch_pairs(plan):
     src_len = (st["end"] - st["begin"]).astype(np.float64)
     cs = np.concatenate([[0.0], np.cumsum(src_len[L["near_list"]])])
     near = cs[L["near_off"][1:]] - cs[L["near_off"][:-1]]
-    return bsz * (near + np.diff(L["far_off"]) * plan.P)
+    return bsz * near, bsz * np.diff(L["far_off"]) * plan.P
+
+
+def cost_model(near, far, secs):
+    """Seconds per near pair and per far pair from per-batch times (least
+    squares, both rates kept non-negative; one shared rate if the fit is not)."""
+    A = np.stack([near, far], 1)
+    coef = np.linalg.lstsq(A, secs, rcond=None)[0]
+    if np.all(coef > 0):
+        return coef
+    r = secs.sum() / (near + far).sum()
+    return np.array([r, r])
 
 
 def stratified_batches(pairs_b, count):
@@ -282,8 +293,14 @@ def stratified_batches(pairs_b, count):
 class CpuTreecode:
     """The oracle's FP64 treecode for one workload: the plan (timed once),
     a fixed stratified sample of target batches, and per-orbital samples
-    extrapolated by pair count.  Both the reference arm and the GPU arm's
-    cpu_baseline leg use this, so they time the same thing."""
+    extrapolated to the whole convolution.  Both the reference arm and the GPU
+    arm's cpu_baseline leg use this, so they time the same thing.
+
+    Extrapolation: each sampled batch's own seconds give a per-pair cost of
+    near pairs and of far pairs (least squares over the sample); the whole
+    convolution's fields cost those rates times all near and far pairs, in
+    thread-seconds, divided by the threads (a few dozen batches over many
+    threads are load-imbalanced, the whole job's thousands are not)."""
 
     def __init__(self, wl, threads, leaf=None, nbatches=CPU_SAMPLE_BATCHES):
         from oracle import oracle as O
@@ -294,29 +311,34 @@ class CpuTreecode:
         t0 = time.perf_counter()
         self.plan = O.Plan(mesh.x, mesh.y, mesh.z, mesh.x, mesh.y, mesh.z, mesh.w, THETA, DEGREE, sl, tl, 1.0)
         self.plan_s = time.perf_counter() - t0
-        self.pairs_b = batch_pairs(self.plan)
+        self.near_b, self.far_b = batch_pairs(self.plan)
+        self.pairs_b = self.near_b + self.far_b
         self.total_pairs = float(self.pairs_b.sum())
         self.sel = stratified_batches(self.pairs_b, nbatches)
         self.halves = (self.sel[0::2], self.sel[1::2])
 
+    def _fields_s(self, sel, secs):
+        a, c = cost_model(self.near_b[sel], self.far_b[sel], secs)
+        return (a * self.near_b.sum() + c * self.far_b.sum()) / self.threads
+
     def orbital(self, o):
         """Seconds of one orbital's convolution (upward pass in full, fields
-        extrapolated from the two halves of the sample) and the two halves'
-        own estimates (their difference is the sample's spread)."""
+        extrapolated from the sample) and the estimates from the sample's two
+        halves alone (their difference is the sample's spread)."""
         O, wl, mesh = self.O, self.wl, self.wl["mesh"]
         q = wl["values"][o]
         kp = wl["kparams"][o]
-        est, t_f, frac, t_up = [], 0.0, 0.0, 0.0
-        for half in self.halves:
-            _, (tu, tf), (pn, pf) = O.convolve_batches(self.plan, q, q, mesh.w, wl["kernel"], kp,
-                                                       wl["singularity"], half, self.threads)
-            fr = (pn + pf) / self.total_pairs
-            est.append(tu + tf / fr)
-            t_f += tf
-            frac += fr
-            t_up = tu
-        return t_up + t_f / frac, est, dict(upward_s=t_up, sample_field_s=t_f, pair_fraction=frac,
-                                            pairs_per_s=frac * self.total_pairs / t_f)
+        _, (t_up, t_f, t_busy), (pn, pf), bs = O.convolve_batches(self.plan, q, q, mesh.w, wl["kernel"], kp,
+                                                                  wl["singularity"], self.sel, self.threads,
+                                                                  per_batch=True)
+        field_s = self._fields_s(self.sel, bs)
+        est = []
+        for h in (0, 1):
+            idx = np.arange(h, len(self.sel), 2)
+            est.append(t_up + self._fields_s(self.sel[idx], bs[idx]))
+        frac = (pn + pf) / self.total_pairs
+        return t_up + field_s, est, dict(upward_s=t_up, sample_thread_s=t_busy, pair_fraction=frac,
+                                         pairs_per_s=self.total_pairs / field_s)
 
     def gram_schmidt_seconds(self, norb):
         """The oracle's FP64 Gram-Schmidt (Orthogonalization.c:14-119 restated)
@@ -351,7 +373,10 @@ def cpu_step_estimate(cpu, norb, orbitals, mgs_s):
 
 def cpu_anchor(threads):
     """One whole FP64 convolution by the oracle, unsampled: the single Z = 4
-    atom, 50,112 points, leaves 500, Yukawa k = 1 with subtraction."""
+    atom, 50,112 points, leaves 500, Yukawa k = 1 with subtraction -- and the
+    same convolution estimated the way the sampled baselines are (plan, one
+    orbital's upward pass, stratified batches, fitted per-pair costs), so the
+    sampling method is checked against a full run."""
     from oracle import oracle as O
     pkg = importlib.import_module(PKG)
     BT = pkg.BaryTreeInterface
@@ -359,7 +384,12 @@ def cpu_anchor(threads):
     t0 = time.perf_counter()
     plan = O.Plan(mesh.x, mesh.y, mesh.z, mesh.x, mesh.y, mesh.z, mesh.w, THETA, DEGREE, PLAIN_LEAF, PLAIN_LEAF, 1.0)
     out = plan.convolve(f, f, mesh.w, BT.Kernel.YUKAWA, [1.0], BT.Singularity.SUBTRACTION, nthreads=threads)
-    return time.perf_counter() - t0, mesh, f, out
+    full_s = time.perf_counter() - t0
+    wl = dict(mesh=mesh, values=f[None, :], kparams=np.array([[1.0]]), kernel=BT.Kernel.YUKAWA,
+              singularity=BT.Singularity.SUBTRACTION, mgs=False)
+    c = CpuTreecode(wl, threads, leaf=(PLAIN_LEAF, PLAIN_LEAF), nbatches=min(CPU_SAMPLE_BATCHES, 24))
+    est, _, _ = cpu_step_estimate(c, 1, [0], 0.0)
+    return full_s, est, mesh, f, out
 
 
 def reference_arm_mesh(args):
@@ -451,7 +481,8 @@ def reference_arm(args):
     sample = (f"FP64 treecode restatement (oracle/tagi_oracle.c, OpenMP, {threads} threads): plan built and timed "
               f"once ({cpu.plan_s:.2f} s); per step one orbital (orbital = step index mod {norb}): upward pass "
               f"in full, fields on a fixed stratified sample of {info['batches']} of {info['of_batches']} target "
-              f"batches ({info['pair_fraction']:.4f} of the pairs), extrapolated by pair count to {norb} orbitals"
+              f"batches ({info['pair_fraction']:.4f} of the pairs), each batch timed: per-pair costs of near and "
+              f"far pairs fitted, applied to all pairs and divided by {threads} threads, times {norb} orbitals"
               + (f"; plus the FP64 Gram-Schmidt of the {norb} orbitals timed in full once ({mgs_s:.2f} s)"
                  if wl["mgs"] else ""))
     line = {"impl": "reference", "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": 0,
@@ -675,7 +706,7 @@ def gb300_arm(args):
         c = CpuTreecode(wl, threads)
         mgs_s = c.gram_schmidt_seconds(norb) if mgs else 0.0
         secs, spread, cinfo = cpu_step_estimate(c, norb, [0], mgs_s)
-        a_s, amesh, af, aout = cpu_anchor(threads)
+        a_s, a_est, amesh, af, aout = cpu_anchor(threads)
         ax, ay, az, aw, aft = (t(v) for v in (amesh.x, amesh.y, amesh.z, amesh.w, af))
         gpu_anchor = {}
         for prec in ("fp64", "mixed"):
@@ -692,13 +723,14 @@ def gb300_arm(args):
                "sample": (f"FP64 treecode restatement (oracle/tagi_oracle.c, OpenMP): plan in full "
                           f"({cinfo['plan_s']:.2f} s), orbital 0's upward pass in full and its fields on a fixed "
                           f"stratified sample of {cinfo['batches']} of {cinfo['of_batches']} target batches "
-                          f"({cinfo['pair_fraction']:.4f} of the pairs), extrapolated by pair count to {norb} "
+                          f"({cinfo['pair_fraction']:.4f} of the pairs; each batch timed, per-pair costs of near and far "
+                          f"pairs fitted, applied to all pairs, divided by {threads} threads), times {norb} "
                           "orbitals" + (f", plus the FP64 Gram-Schmidt of {norb} orbitals in full "
                                         f"({mgs_s:.2f} s, one thread)" if mgs else "")),
                "spread": spread,
                "anchor": {"what": "one whole FP64 convolution, unsampled: single Z = 4 atom, 50,112 points, "
                                   "leaves 500, Yukawa k = 1 with subtraction",
-                          "cpu_seconds": a_s, "gpu": gpu_anchor}}
+                          "cpu_seconds": a_s, "cpu_seconds_estimated_from_a_sample": a_est, "gpu": gpu_anchor}}
 
     line = {
         "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": ws, "steps": args.steps,
@@ -1175,11 +1207,11 @@ def cpu_two_mesh_sample(tab, pts, nuclei, target_seconds, threads):
     ff = np.exp(-np.sqrt((Xf - R[0]) ** 2 + (Yf - R[1]) ** 2 + (Zf - R[2]) ** 2))
     order = np.random.default_rng(17).permutation(nb)
     sel = np.sort(order[:4])
-    _, (t_up, t_f), (pn, pf) = O.convolve_batches(plan, fc, ff, Wf, 2, [1.0], 2, sel, threads)
+    _, (t_up, t_f, _), (pn, pf) = O.convolve_batches(plan, fc, ff, Wf, 2, [1.0], 2, sel, threads)
     want = (pn + pf) / max(t_f, 1e-9) * target_seconds
     nsel = int(np.clip(np.searchsorted(np.cumsum(pairs_b[order]), want) + 1, 4, nb))
     sel = np.sort(order[:nsel])
-    _, (t_up, t_f), (pn, pf) = O.convolve_batches(plan, fc, ff, Wf, 2, [1.0], 2, sel, threads)
+    _, (t_up, t_f, _), (pn, pf) = O.convolve_batches(plan, fc, ff, Wf, 2, [1.0], 2, sel, threads)
     frac = (pn + pf) / pairs_b.sum()
     return t_plan + t_up + t_f / frac, dict(plan_s=t_plan, upward_s=t_up, batches=nsel, of_batches=nb,
                                             pair_fraction=float(frac), pairs_per_s=(pn + pf) / t_f)

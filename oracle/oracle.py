@@ -65,6 +65,9 @@ def lib():
         L.oracle_plan_convolve_batches.argtypes = [ctypes.c_void_p, _dp, _dp, _dp, ctypes.c_int, _dp,
                                                    ctypes.c_int, _dp, ctypes.c_int, ctypes.c_int,
                                                    _ip, _dp, _dp]
+        L.oracle_plan_convolve_batches_timed.argtypes = [ctypes.c_void_p, _dp, _dp, _dp, ctypes.c_int, _dp,
+                                                         ctypes.c_int, _dp, ctypes.c_int, ctypes.c_int,
+                                                         _ip, _dp, _dp, _dp]
         L.oracle_mgs.argtypes = [_dp, _dp, _dp, ctypes.c_int, ctypes.c_int, ctypes.c_int]
         L.oracle_interp.argtypes = [_dp, _dp, _dp, _dp, _ip, ctypes.c_int, _dp, _dp, _dp, _dp,
                                     _ip, ctypes.c_int, ctypes.c_int, ctypes.c_int]
@@ -169,17 +172,23 @@ class Plan:
         return out
 
 
-def convolve_batches(plan, tv, sv, sw, kernel, kparams, singularity, batches, nthreads=0):
-    """Convolve only the listed batches; returns (out, (t_upward, t_fields), (near, far pairs))."""
+def convolve_batches(plan, tv, sv, sw, kernel, kparams, singularity, batches, nthreads=0, per_batch=False):
+    """Convolve only the listed batches; returns (out, (t_upward, t_fields, thread_seconds_fields),
+    (near, far pairs)): wall seconds of the upward pass and of the fields, and the fields' time
+    summed over the batches (per-thread busy time, independent of load imbalance).  With
+    per_batch, a fourth item: each listed batch's own seconds."""
     tv, sv, sw = _c(tv), _c(sv), _c(sw)
     kp = _c(np.atleast_1d(kparams))
     sel = _c(batches, np.int32)
     out = np.zeros(plan.nt)
-    times = np.zeros(2)
+    times = np.zeros(3)
     pairs = np.zeros(2)
-    lib().oracle_plan_convolve_batches(plan.h, _p(tv), _p(sv), _p(sw), int(kernel), _p(kp),
-                                       int(singularity), _p(out), nthreads, len(sel), _p(sel, _ip),
-                                       _p(times), _p(pairs))
+    bs = np.zeros(max(len(sel), 1))
+    lib().oracle_plan_convolve_batches_timed(plan.h, _p(tv), _p(sv), _p(sw), int(kernel), _p(kp),
+                                             int(singularity), _p(out), nthreads, len(sel), _p(sel, _ip),
+                                             _p(times), _p(pairs), _p(bs))
+    if per_batch:
+        return out, tuple(times), tuple(pairs), bs[: len(sel)]
     return out, tuple(times), tuple(pairs)
 
 

@@ -536,10 +536,26 @@ static double wall_s(void)
  * phi_i = near(direct) + far(proxy) + SS term.  times[0] = upward pass s,
  * times[1] = field s; pairs[0] = near pairs, pairs[1] = far pairs (selected).
  */
+void oracle_plan_convolve_batches_timed(void *vp, const double *tv, const double *sv, const double *sw,
+                                        int kernel, const double *kparams, int sing, double *out,
+                                        int nthreads, int nsel, const int *sel, double *times,
+                                        double *pairs, double *batch_s);
+
 void oracle_plan_convolve_batches(void *vp, const double *tv, const double *sv, const double *sw,
                                   int kernel, const double *kparams, int sing, double *out,
                                   int nthreads, int nsel, const int *sel, double *times,
                                   double *pairs)
+{
+    oracle_plan_convolve_batches_timed(vp, tv, sv, sw, kernel, kparams, sing, out, nthreads, nsel, sel,
+                                       times, pairs, NULL);
+}
+
+/* As oracle_plan_convolve_batches; batch_s (if not NULL) receives each
+ * evaluated batch's own seconds, in the order of sel. */
+void oracle_plan_convolve_batches_timed(void *vp, const double *tv, const double *sv, const double *sw,
+                                        int kernel, const double *kparams, int sing, double *out,
+                                        int nthreads, int nsel, const int *sel, double *times,
+                                        double *pairs, double *batch_s)
 {
     oplan *p = (oplan *)vp;
     const otree *s = &p->src, *t = &p->tgt;
@@ -567,11 +583,12 @@ void oracle_plan_convolve_batches(void *vp, const double *tv, const double *sv, 
     cheb2_nodes(p->degree, tn);
     int sing_ss = (sing == S_SUBTRACTION);
     int nrun = sel ? nsel : p->nbatch;
-    double npairs = 0.0, fpairs = 0.0;
+    double npairs = 0.0, fpairs = 0.0, busy = 0.0;
 #ifdef _OPENMP
-#pragma omp parallel for schedule(dynamic, 1) reduction(+ : npairs, fpairs)
+#pragma omp parallel for schedule(dynamic, 1) reduction(+ : npairs, fpairs, busy)
 #endif
     for (int bi = 0; bi < nrun; bi++) {
+        double tb = wall_s();
         int b = sel ? sel[bi] : bi;
         int bn = p->batch_node[b];
         int nb = t->end[bn] - t->begin[bn];
@@ -619,9 +636,13 @@ void oracle_plan_convolve_batches(void *vp, const double *tv, const double *sv, 
             }
             out[oi] = acc + ss_term(kernel, sing, kp, fi);
         }
+        double dt = wall_s() - tb;
+        busy += dt;
+        if (batch_s) batch_s[bi] = dt;
     }
     double t2 = wall_s();
-    if (times) { times[0] = t1 - t0; times[1] = t2 - t1; }
+    /* times: upward pass (wall), fields (wall), fields summed over the batches (thread-seconds) */
+    if (times) { times[0] = t1 - t0; times[1] = t2 - t1; times[2] = busy; }
     if (pairs) { pairs[0] = npairs; pairs[1] = fpairs; }
     free(qs); free(ws); free(fs); free(qhat);
 }
