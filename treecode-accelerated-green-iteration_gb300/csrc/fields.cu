@@ -360,13 +360,14 @@ __global__ void __launch_bounds__(FT, TAGI_NEAR_MINB) near_mixed(const __grid_co
 template <int MAXN1>
 __host__ __device__ constexpr int even_up() { return MAXN1 + (MAXN1 & 1); }
 
-template <int KERN, bool SS, bool EXPTERM, int MAXN1, int NT>
+template <int KERN, bool SS, bool EXPTERM, int MAXN1, int NT, bool EXACT = false>
 __device__ __forceinline__ void far_cluster(const float *__restrict__ s_q, const float *__restrict__ s_w,
-                                            const float (*s_p)[MAXN1], int n1, const float (&tx)[NT],
+                                            const float (*s_p)[MAXN1], int n1_in, const float (&tx)[NT],
                                             const float (&ty)[NT], const float (&tz)[NT],
                                             const float2 (&nfi)[NT], float (&sum)[NT], float (&cmp)[NT]) {
     constexpr int MH = even_up<MAXN1>() / 2;
     constexpr bool PSS = KERN == KERNEL_YUKAWA ? SS : (SS && EXPTERM);
+    const int n1 = EXACT ? MAXN1 : n1_in;   // EXACT: every loop bound known at compile time
     const int n1p = n1 + (n1 & 1);
     float2 dz2[NT][MH];
 #pragma unroll
@@ -410,7 +411,9 @@ __device__ __forceinline__ void far_cluster(const float *__restrict__ s_q, const
     }
 }
 
-template <int KERN, bool SS, int MAXN1, int NT>
+// EXACT: every system of the launch has n + 1 = MAXN1 (the loops over the
+// proxy grid are then fully known at compile time).
+template <int KERN, bool SS, int MAXN1, int NT, bool EXACT = false>
 __global__ void __launch_bounds__(FT, 2) far_mixed(const __grid_constant__ Work w) {
     constexpr int MAXPP = MAXN1 * MAXN1 * even_up<MAXN1>();
     __shared__ __align__(16) float s_q[MAXPP];
@@ -424,7 +427,7 @@ __global__ void __launch_bounds__(FT, 2) far_mixed(const __grid_constant__ Work 
         const int2 it = w.items[item];
         const Fields &a = w.sys[it.y >> 16];
         const int b = it.x, orb = it.y & 0xffff;
-        const int n1 = a.n1, P = a.P;
+        const int n1 = EXACT ? MAXN1 : a.n1, P = EXACT ? MAXN1 * MAXN1 * MAXN1 : a.P;
         const int n1p = n1 + (n1 & 1), Pp = n1 * n1 * n1p;
         const int f0 = a.far_off[b], f1 = a.far_off[b + 1];
         if (f0 == f1) continue;
@@ -484,9 +487,9 @@ __global__ void __launch_bounds__(FT, 2) far_mixed(const __grid_constant__ Work 
                 const int mode = s_mode;
                 if (mode == 2 || !warp_busy) continue;
                 if (mode == 1)
-                    far_cluster<KERN, SS, false, MAXN1, NT>(s_q, s_w, s_p, n1, tx, ty, tz, nfi, sum, cmp);
+                    far_cluster<KERN, SS, false, MAXN1, NT, EXACT>(s_q, s_w, s_p, n1, tx, ty, tz, nfi, sum, cmp);
                 else
-                    far_cluster<KERN, SS, true, MAXN1, NT>(s_q, s_w, s_p, n1, tx, ty, tz, nfi, sum, cmp);
+                    far_cluster<KERN, SS, true, MAXN1, NT, EXACT>(s_q, s_w, s_p, n1, tx, ty, tz, nfi, sum, cmp);
             }
 #pragma unroll
             for (int k = 0; k < NT; k++) {
@@ -509,7 +512,7 @@ __global__ void __launch_bounds__(FT, 2) far_mixed(const __grid_constant__ Work 
 // Orbitals past the last one of the request have zero charges and are not
 // written.
 // ---------------------------------------------------------------------------
-constexpr int GTILE = 256;   // sources per group tile
+constexpr int GTILE = 512;   // sources per group tile
 
 __device__ __forceinline__ int q4_pos(int j, int o, int og) {   // float index of q(o, j) in the staged layout
     return (((j >> 1) * (og >> 1) + (o >> 1)) << 2) + ((o & 1) << 1) + (j & 1);
@@ -527,7 +530,7 @@ __device__ __forceinline__ void group_tile(const float (*__restrict__ s)[GTILE],
         float2 part[OG];
 #pragma unroll
         for (int o = 0; o < OG; o++) part[o] = make_float2(0.f, 0.f);
-#pragma unroll 2
+#pragma unroll 1   // measured: unrolling the source loop slows the group kernels
         for (int j = j0; j < j1; j += 2) {
             float2 dx = add2(tx, lds2(s[0] + j)), dy = add2(ty, lds2(s[1] + j)), dz = add2(tz, lds2(s[2] + j));
             if constexpr (PRECISE) {
@@ -673,12 +676,13 @@ __global__ void __launch_bounds__(FT, 2) near_group(const __grid_constant__ Work
 
 // One staged proxy grid against one target for a group of orbitals (see
 // far_cluster for the padded innermost axis).
-template <bool SS, int MAXN1, int OG>
+template <bool SS, int MAXN1, int OG, bool EXACT = false>
 __device__ __forceinline__ void far_group_cluster(const float4 *__restrict__ s_q4, const float *__restrict__ s_w,
-                                                  const float (*s_p)[MAXN1], int n1, float tx, float ty, float tz,
+                                                  const float (*s_p)[MAXN1], int n1_in, float tx, float ty, float tz,
                                                   const float2 (&nfi)[OG], const float2 (&kc)[OG],
                                                   const float2 (&kl)[OG], float (&sum)[OG], float (&cmp)[OG]) {
     constexpr int MH = even_up<MAXN1>() / 2;
+    const int n1 = EXACT ? MAXN1 : n1_in;
     const int n1p = n1 + (n1 & 1);
     float2 dz2[MH];
 #pragma unroll
@@ -731,7 +735,7 @@ __host__ __device__ constexpr size_t far_group_smem(int n1, int og) {
     return sizeof(float) * (size_t)n1 * n1 * (n1 + (n1 & 1)) * (og + 1);
 }
 
-template <bool SS, int MAXN1, int OG>
+template <bool SS, int MAXN1, int OG, bool EXACT = false>
 __global__ void __launch_bounds__(FT, 2) far_group(const __grid_constant__ Work w) {
     extern __shared__ __align__(16) float s_dyn[];
     __shared__ float s_p[3][MAXN1];
@@ -744,7 +748,7 @@ __global__ void __launch_bounds__(FT, 2) far_group(const __grid_constant__ Work 
         const int2 it = w.items[item];
         const Fields &a = w.sys[it.y >> 16];
         const int b = it.x, g0 = it.y & 0xffff;
-        const int n1 = a.n1, P = a.P;
+        const int n1 = EXACT ? MAXN1 : a.n1, P = EXACT ? MAXN1 * MAXN1 * MAXN1 : a.P;
         const int n1p = n1 + (n1 & 1), Pp = n1 * n1 * n1p;
         const float *s_w = s_dyn + (size_t)Pp * OG;   // Pp * OG is a multiple of 4: float4 aligned
         const int f0 = a.far_off[b], f1 = a.far_off[b + 1];
@@ -798,7 +802,7 @@ __global__ void __launch_bounds__(FT, 2) far_group(const __grid_constant__ Work 
                 }
                 __syncthreads();
                 if (!warp_busy) continue;
-                far_group_cluster<SS, MAXN1, OG>(s_q4, s_w, s_p, n1, tx, ty, tz, nfi, kc, kl, sum, cmp);
+                far_group_cluster<SS, MAXN1, OG, EXACT>(s_q4, s_w, s_p, n1, tx, ty, tz, nfi, kc, kl, sum, cmp);
             }
             if (v) {
 #pragma unroll
@@ -1067,7 +1071,7 @@ __global__ void __launch_bounds__(FT) pair_peak_far(int reps, float *out) {
         nfi[k] = dup2(-0.3f);
     }
     for (int r = 0; r < reps; r++)
-        far_cluster<KERN, SS, true, N1, 2>(s_q, s_w, s_p, N1, tx, ty, tz, nfi, sum, cmp);
+        far_cluster<KERN, SS, true, N1, 2, true>(s_q, s_w, s_p, N1, tx, ty, tz, nfi, sum, cmp);
     out[blockIdx.x * FT + threadIdx.x] = sum[0] + sum[1] - cmp[0] - cmp[1];
 }
 
@@ -1131,7 +1135,7 @@ __global__ void __launch_bounds__(FT, 2) pair_peak_far_group(int reps, float *ou
         sum[o] = cmp[o] = 0.f;
     }
     for (int r = 0; r < reps; r++)
-        far_group_cluster<SS, N1, OG>(s_q4, s_w, s_p, N1, tx, ty, tz, nfi, kc, kl, sum, cmp);
+        far_group_cluster<SS, N1, OG, true>(s_q4, s_w, s_p, N1, tx, ty, tz, nfi, kc, kl, sum, cmp);
     float acc = 0.f;
 #pragma unroll
     for (int o = 0; o < OG; o++) acc += sum[o] - cmp[o];
@@ -1193,7 +1197,8 @@ int run_pair_peak(int variant, double *pairs_per_s, cudaStream_t s) {
 struct LaunchShape {
     int og = 1;     // orbitals per item (orbital-group kernels) or 1
     int nt = 1;     // targets per thread: 2 when some batch holds more than FT targets
-    int maxn1 = 1;  // largest proxy-grid edge n + 1
+    int maxn1 = 1;        // largest proxy-grid edge n + 1
+    int minn1 = 1 << 20;  // smallest proxy-grid edge n + 1
 };
 
 template <int KERN, bool SS>
@@ -1233,6 +1238,9 @@ int launch_fields(const SysCall *calls, const Fields *f, int nsys, const Schedul
         if (sh.maxn1 <= 4) {
             if (g8) TAGI_TRY(launch_persistent(far_group<SS, 4, 8>, wf, s, fsm));
             else TAGI_TRY(launch_persistent(far_group<SS, 4, 4>, wf, s, fsm));
+        } else if (sh.maxn1 == 8 && sh.minn1 == 8) {   // degree 7 everywhere: loops known at compile time
+            if (g8) TAGI_TRY(launch_persistent(far_group<SS, 8, 8, true>, wf, s, fsm));
+            else TAGI_TRY(launch_persistent(far_group<SS, 8, 4, true>, wf, s, fsm));
         } else if (sh.maxn1 <= 8) {
             if (g8) TAGI_TRY(launch_persistent(far_group<SS, 8, 8>, wf, s, fsm));
             else TAGI_TRY(launch_persistent(far_group<SS, 8, 4>, wf, s, fsm));
@@ -1258,12 +1266,15 @@ int launch_fields(const SysCall *calls, const Fields *f, int nsys, const Schedul
     }
     phase_mark(PH_FAR, true, s);
     if (precision == PREC_MIXED) {
+        const bool deg7 = sh.maxn1 == 8 && sh.minn1 == 8;
         if (one) {
             if (sh.maxn1 <= 4) TAGI_TRY(launch_persistent(far_mixed<KERN, SS, 4, 1>, wf, s));
+            else if (deg7) TAGI_TRY(launch_persistent(far_mixed<KERN, SS, 8, 1, true>, wf, s));
             else if (sh.maxn1 <= 8) TAGI_TRY(launch_persistent(far_mixed<KERN, SS, 8, 1>, wf, s));
             else TAGI_TRY(launch_persistent(far_mixed<KERN, SS, MAX_DEGREE + 1, 1>, wf, s));
         } else {
             if (sh.maxn1 <= 4) TAGI_TRY(launch_persistent(far_mixed<KERN, SS, 4, 2>, wf, s));
+            else if (deg7) TAGI_TRY(launch_persistent(far_mixed<KERN, SS, 8, 2, true>, wf, s));
             else if (sh.maxn1 <= 8) TAGI_TRY(launch_persistent(far_mixed<KERN, SS, 8, 2>, wf, s));
             else TAGI_TRY(launch_persistent(far_mixed<KERN, SS, MAX_DEGREE + 1, 2>, wf, s));
         }
@@ -1515,6 +1526,7 @@ int convolve_systems(SysCall *calls, int nsys, int kernel, int singularity, int 
         f[i] = make_fields(p, c.norb);
         if (p.max_batch > FT) sh.nt = 2;  // automatic: two targets per thread for batches above FT
         if (p.n1 > sh.maxn1) sh.maxn1 = p.n1;
+        if (p.n1 < sh.minn1) sh.minn1 = p.n1;
         // the far and close-range passes write only the batches they visit
         TAGI_CUDA(cudaMemsetAsync(p.far_out, 0, sizeof(double) * (size_t)c.norb * nt, s));
         TAGI_CUDA(cudaMemsetAsync(p.near2_out, 0, sizeof(double) * (size_t)c.norb * nt, s));
