@@ -22,6 +22,15 @@
  * treated as SKIPPING: coincident pairs are left out), LAGRANGE,
  * PARTICLE_CLUSTER, degree 1..10.  Anything else returns TAGI_ERR_UNSUPPORTED.
  *
+ * Kernel parameters: COULOMB and YUKAWA read kernelParameters[0] (k for
+ * Yukawa, the Gaussian exponent alpha for Coulomb subtraction) and accept
+ * numberOfKernelParameters >= 1; further values are ignored.  TAGI's
+ * regularize=True call form passes Kernel.YUKAWA with two parameters [k,
+ * epsilon] (greenIterationFixedPoint.py:223-227, scfFixedPoint.py:246-250,
+ * where the caller itself warns if epsilon != 0): that call gives exactly the
+ * one-parameter result.  REGULARIZED_COULOMB / REGULARIZED_YUKAWA (kernel 3 /
+ * 4), the kernels that would use epsilon, return TAGI_ERR_UNSUPPORTED.
+ *
  * Precision: TAGI_PREC_MIXED (FP32 pair sums with compensated accumulation,
  * FP64 singularity term) or TAGI_PREC_FP64.
  */

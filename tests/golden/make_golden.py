@@ -17,7 +17,8 @@ import numpy as np
 
 HERE = os.path.dirname(os.path.abspath(__file__))
 ROOT = os.path.dirname(os.path.dirname(HERE))
-REF_UTIL = "/root/reference/3D-GreenIteration/src/utilities"
+REF_ROOT = os.environ.get("TAGI_REFERENCE", "/root/reference")   # the reference repository's root
+REF_UTIL = os.path.join(REF_ROOT, "3D-GreenIteration", "src", "utilities")
 sys.path.insert(0, ROOT)
 
 from oracle import oracle as O  # noqa: E402
@@ -138,7 +139,7 @@ def mesh_golden(mu):
     np.savez_compressed(os.path.join(HERE, "mesh_reference.npz"), **out)
 
 
-REF_DATA = "/root/reference/3D-GreenIteration/src/dataStructures"
+REF_DATA = os.path.join(REF_ROOT, "3D-GreenIteration", "src", "dataStructures")
 
 
 def reference_mesh_building():
