@@ -223,6 +223,30 @@ class GreenIteration:
         if self.anderson is not None:
             self.anderson["count"] = 0
 
+    def anderson_checkpoint(self):
+        """The part of the mixing history the next anderson_step may change
+        (its count and the ring row it writes), copied; None without mixing."""
+        a = self.anderson
+        if a is None:
+            return None
+        row = a["count"] % a["H"]
+        with torch.cuda.stream(self.stream):
+            return dict(count=a["count"], mixed=a["mixed"], row=row, X=a["X"][row].clone(), F=a["F"][row].clone(),
+                        ex=a["ex"][row].copy(), ef=a["ef"][row].copy())
+
+    def anderson_restore(self, ck):
+        """Undo the mixing-history changes made since anderson_checkpoint: the
+        history is again exactly the plain method's."""
+        a = self.anderson
+        if a is None or ck is None:
+            return
+        r = ck["row"]
+        with torch.cuda.stream(self.stream):
+            a["X"][r].copy_(ck["X"])
+            a["F"][r].copy_(ck["F"])
+        a["ex"][r], a["ef"][r] = ck["ex"], ck["ef"]
+        a["count"], a["mixed"] = ck["count"], ck["mixed"]
+
     def anderson_step(self, residual):
         """Mix after a sweep (the stream must be idle); returns True if it mixed."""
         a = self.anderson

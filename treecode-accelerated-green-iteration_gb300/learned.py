@@ -136,8 +136,10 @@ class MLP:
 class LearnedExtrapolator:
     """Online-trained extrapolation of Green-iteration sweeps (see module doc).
 
-    P: points per cell (the mesh stores cells contiguously); rollout: predicted
-    steps per proposal; train_steps: Adam steps per new training pair; warmup:
+    P: points per cell (the mesh stores cells contiguously); rollout: the
+    largest number of predicted steps per proposal (the length adapts: it
+    starts at 2, doubles after a kept jump up to `rollout`, halves after a
+    rejected one down to 1); train_steps: Adam steps per new training pair; warmup:
     training pairs seen before the first proposal; cooldown: sweeps without
     proposals after a rejected one (doubling on repeated rejections).
 
@@ -151,6 +153,7 @@ class LearnedExtrapolator:
     def __init__(self, P, hidden=256, rollout=6, train_steps=4, warmup=2, cooldown=2, lr=1e-3, floor=1e-3,
                  seed=0, correction=1.0, min_residual=0.0):
         self.P, self.rollout, self.train_steps = int(P), int(rollout), int(train_steps)
+        self.steps = min(2, self.rollout)   # current rollout length
         # weight of the network's correction to the learned skip term, and the residual below
         # which no more proposals are made (plain sweeps finish the convergence)
         self.correction, self.min_residual = float(correction), float(min_residual)
@@ -160,12 +163,15 @@ class LearnedExtrapolator:
         self.disabled = False  # set for the rest of the run when too few jumps are kept
         self.gate = None  # running ratio of validation losses: full network / skip term alone
         self.stats = dict(proposals=0, accepted=0, rejected=0, trained=0, sweeps=0, extra_sweeps=0)
+        self.log = []   # per proposal: rollout, residual before, residual after, kept
         self.reset()
 
     def reset(self):
-        """Forget the iterate history (new potential or reordered orbitals); keep the weights."""
+        """Forget the iterate history (new potential or reordered orbitals); keep the weights,
+        which go on training across potentials."""
         self.hist = []          # device copies of the last plain iterates (psi)
         self.eps_hist = []      # host copies of their eigenvalues
+        self.anderson_ck = None
         self.pending = False
         self.cool = 0
         self.backoff = self.cooldown_len
@@ -224,8 +230,11 @@ class LearnedExtrapolator:
         """psi <- psi_t + sum of `rollout` predicted updates, Gram-Schmidt'ed; backup kept."""
         L = _native.lib()
         s = ctypes.c_void_p(gi.stream.cuda_stream)
-        if hasattr(gi, "reset_anderson"):
-            gi.reset_anderson()  # a jump breaks the sweep history that orbital mixing works on
+        # Orbital mixing keeps its history across a jump: the sweep from the
+        # proposal adds a genuine (input, output) pair to it.  If the jump is
+        # rejected that pair is taken out again, so the plain method resumes
+        # with exactly its own history.
+        self.anderson_ck = gi.anderson_checkpoint() if hasattr(gi, "anderson_checkpoint") else None
         self.backup_psi.copy_(gi.psi)
         self.backup_eps.copy_(gi.eps)
         self.work_psi.copy_(gi.psi)
@@ -234,10 +243,10 @@ class LearnedExtrapolator:
         d1, d2 = e1 - e0, e2 - e1
         with np.errstate(divide="ignore", invalid="ignore"):
             rho = np.clip(np.where(np.abs(d1) > 0, d2 / d1, 0.0), 0.0, 0.9)
-        J = self.rollout
+        J = self.steps
         self.eps_proposed = e2 + d2 * rho * (1.0 - rho ** J) / (1.0 - rho)
         torch.sub(self.hist[-1], self.hist[-2], out=self.work_d)
-        for _ in range(self.rollout):
+        for _ in range(J):
             self._features(gi, self.work_psi, self.work_d)
             Y = self.net.forward(self.X, self.rows)
             # the network's correction is used only while it beats its own skip term on unseen pairs
@@ -265,7 +274,13 @@ class LearnedExtrapolator:
             self.stats["sweeps"] += 1
             if self.pending:
                 self.pending = False
-                if self.last_res is not None and res < self.last_res:
+                kept = self.last_res is not None and res < self.last_res
+                self.log.append((self.steps, self.last_res, res, kept, self.gate))
+                if kept:
+                    self.steps = min(2 * self.steps, self.rollout)
+                else:
+                    self.steps = max(self.steps // 2, 1)
+                if kept:
                     self.stats["accepted"] += 1
                     # the jump's sweep is a plain update from the proposal: restart the history there
                     self.hist = [self.work_psi.clone(), gi.psi.clone()]
@@ -278,8 +293,8 @@ class LearnedExtrapolator:
                 self.stats["extra_sweeps"] += 1
                 gi.psi.copy_(self.backup_psi)
                 gi.set_eigenvalues(self.backup_eps.cpu().numpy())
-                if hasattr(gi, "reset_anderson"):
-                    gi.reset_anderson()
+                if hasattr(gi, "anderson_restore"):
+                    gi.anderson_restore(self.anderson_ck)
                 self.cool = self.backoff
                 self.backoff = min(2 * self.backoff + 1, 16)
                 scf._gi_sweep()
