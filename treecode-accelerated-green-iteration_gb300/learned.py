@@ -138,8 +138,9 @@ class LearnedExtrapolator:
 
     P: points per cell (the mesh stores cells contiguously); rollout: the
     largest number of predicted steps per proposal (the length adapts: it
-    starts at 2, doubles after a kept jump up to `rollout`, halves after a
-    rejected one down to 1); train_steps: Adam steps per new training pair; warmup:
+    starts at `rollout`, halves after a rejected jump down to 1 and doubles
+    after a kept one back up to `rollout`); train_steps: Adam steps per new
+    training pair; warmup:
     training pairs seen before the first proposal; cooldown: sweeps without
     proposals after a rejected one (doubling on repeated rejections).
 
@@ -153,7 +154,7 @@ class LearnedExtrapolator:
     def __init__(self, P, hidden=256, rollout=6, train_steps=4, warmup=2, cooldown=2, lr=1e-3, floor=1e-3,
                  seed=0, correction=1.0, min_residual=0.0):
         self.P, self.rollout, self.train_steps = int(P), int(rollout), int(train_steps)
-        self.steps = min(2, self.rollout)   # current rollout length
+        self.steps = self.rollout   # current rollout length
         # weight of the network's correction to the learned skip term, and the residual below
         # which no more proposals are made (plain sweeps finish the convergence)
         self.correction, self.min_residual = float(correction), float(min_residual)
