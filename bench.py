@@ -1319,7 +1319,7 @@ def twomesh_arm(args):
             "roofline": {"bound": "fp32" if t_fma >= t_mufu else "mufu",
                          "kernel": f"{dominant} field: {dominant}_mixed (Hartree) + {dominant}_group (21 Yukawa "
                                    "orbitals, groups of 8)",
-                         "achieved": achieved / 1e9, "peak": achieved / 1e9 * bound_ms / k_ms,
+                         "achieved": achieved / 1e9, "peak": achieved / 1e9 * k_ms / bound_ms,
                          "unit": "Gpair-orbitals/s", "frac": bound_ms / k_ms, "traffic": None,
                          "pipe_frac": {"fp32": t_fma * 1e3 / k_ms, "mufu": t_mufu * 1e3 / k_ms},
                          "peak_source": "hardware pipe rates measured live (tagi_pipe_rates) and the kernels' "
