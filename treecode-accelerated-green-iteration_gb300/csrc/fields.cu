@@ -814,6 +814,112 @@ __global__ void __launch_bounds__(FT, 2) far_group(const __grid_constant__ Work 
 }
 
 // ---------------------------------------------------------------------------
+// far_group at degree 7 with the next cluster's charges in flight: cp.async
+// copies global -> shared without registers, so the charges and weight
+// charges of far cluster e+1 load while cluster e is computed, and one
+// barrier per cluster separates the two buffers.  Charges are copied 8 bytes
+// at a time ({q(o, j), q(o, j+1)} is contiguous both in global memory and in
+// the staged layout); orbitals past the request's last get zero-filled copies.
+// ---------------------------------------------------------------------------
+__device__ __forceinline__ void cp_async8(void *smem, const void *gmem, bool valid) {
+    const unsigned sa = (unsigned)__cvta_generic_to_shared(smem);
+    const int n = valid ? 8 : 0;   // source bytes; the rest of the 8 are zero-filled
+    asm volatile("cp.async.ca.shared.global [%0], [%1], 8, %2;\n" ::"r"(sa), "l"(gmem), "r"(n) : "memory");
+}
+__device__ __forceinline__ void cp_async16(void *smem, const void *gmem) {
+    const unsigned sa = (unsigned)__cvta_generic_to_shared(smem);
+    asm volatile("cp.async.cg.shared.global [%0], [%1], 16;\n" ::"r"(sa), "l"(gmem) : "memory");
+}
+__device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;\n" ::: "memory"); }
+__device__ __forceinline__ void cp_async_wait_all() { asm volatile("cp.async.wait_group 0;\n" ::: "memory"); }
+
+constexpr int DB_N1 = 8, DB_P = DB_N1 * DB_N1 * DB_N1;   // degree 7
+__host__ __device__ constexpr size_t far_group_db_smem(int og) { return sizeof(float) * 2 * (size_t)DB_P * (og + 1); }
+
+template <bool SS, int OG>
+__global__ void __launch_bounds__(FT, 2) far_group_db(const __grid_constant__ Work w) {
+    constexpr int BUF = DB_P * OG + DB_P;   // floats per buffer: charges, then weight charges
+    extern __shared__ __align__(16) float s_dyn[];
+    __shared__ float s_p[2][3][DB_N1];
+    __shared__ int s_item;
+    const int tid = threadIdx.x;
+    for (;;) {
+        const int item = next_item(w.queue, &s_item);
+        if (item >= w.nitems) break;
+        const int2 it = w.items[item];
+        const Fields &a = w.sys[it.y >> 16];
+        const int b = it.x, g0 = it.y & 0xffff;
+        const int f0 = a.far_off[b], f1 = a.far_off[b + 1];
+        if (f0 == f1) continue;
+        const int bn = a.batch_node[b];
+        const int tb = a.tbegin[bn], te = a.tend[bn];
+        const double cb[3] = {a.tcenter[3L * bn], a.tcenter[3L * bn + 1], a.tcenter[3L * bn + 2]};
+        float2 kc[OG], kl[OG];
+#pragma unroll
+        for (int o = 0; o < OG; o++) {
+            float h, l;
+            split_f32((g0 + o) < a.norb ? -a.kp64[g0 + o] * LOG2E : 0.0, h, l);
+            kc[o] = dup2(h);
+            kl[o] = dup2(l);
+        }
+        // issue the copies of far cluster e into buffer buf (completes at the next wait + barrier)
+        auto stage = [&](int e, int buf) {
+            const int slot = a.node_slot[a.far_list[e]];
+            float *q = s_dyn + (size_t)buf * BUF;
+            for (int k = tid; k < DB_P * OG / 2; k += FT) {
+                const int o = k / (DB_P / 2), kk = 2 * (k - o * (DB_P / 2));
+                const int orb = g0 + o;
+                const bool valid = orb < a.norb;
+                const float *src = a.qhat32 + ((long)(valid ? orb : g0) * a.nslots + slot) * DB_P + kk;
+                cp_async8(q + q4_pos(kk, o, OG), src, valid);
+            }
+            for (int k = tid; k < DB_P / 4; k += FT) cp_async16(q + DB_P * OG + 4 * k, a.what32 + (long)slot * DB_P + 4 * k);
+            cp_async_commit();
+            if (tid < 3 * DB_N1) {
+                const double *gm = a.geom + 6L * slot;
+                const int d = tid / DB_N1, m = tid - d * DB_N1;
+                const double cbd = d == 0 ? cb[0] : (d == 1 ? cb[1] : cb[2]);
+                s_p[buf][d][m] = (float)((gm[d] + gm[3 + d] * a.tn[m]) - cbd);
+            }
+        };
+        for (int base = tb; base < te; base += FT) {
+            const int i = base + tid;
+            const bool v = i < te;
+            const bool warp_busy = base + (tid & ~31) < te;
+            const float tx = v ? (float)(a.tx[i] - cb[0]) : 0.f;
+            const float ty = v ? (float)(a.ty[i] - cb[1]) : 0.f;
+            const float tz = v ? (float)(a.tz[i] - cb[2]) : 0.f;
+            float2 nfi[OG];
+            float sum[OG], cmp[OG];
+#pragma unroll
+            for (int o = 0; o < OG; o++) {
+                const int orb = g0 + o;
+                nfi[o] = dup2((v && orb < a.norb) ? -a.ft32[(long)orb * a.nt + i] : 0.f);
+                sum[o] = 0.f;
+                cmp[o] = 0.f;
+            }
+            __syncthreads();   // every thread is done with both buffers of the previous target chunk
+            stage(f0, 0);
+            for (int e = f0; e < f1; e++) {
+                const int cur = (e - f0) & 1;
+                cp_async_wait_all();   // this thread's copies of cluster e
+                __syncthreads();       // everyone's copies visible; everyone done reading the other buffer
+                if (e + 1 < f1) stage(e + 1, cur ^ 1);
+                if (!warp_busy) continue;
+                const float *q = s_dyn + (size_t)cur * BUF;
+                far_group_cluster<SS, DB_N1, OG, true>(reinterpret_cast<const float4 *>(q), q + DB_P * OG, s_p[cur],
+                                                       DB_N1, tx, ty, tz, nfi, kc, kl, sum, cmp);
+            }
+            if (v) {
+#pragma unroll
+                for (int o = 0; o < OG; o++)
+                    if (g0 + o < a.norb) a.out[(long)(g0 + o) * a.nt + i] = (double)sum[o] - (double)cmp[o];
+            }
+        }
+    }
+}
+
+// ---------------------------------------------------------------------------
 // FP64 near and far fields (the plain path).
 // ---------------------------------------------------------------------------
 template <int KERN, bool SS>
@@ -1238,9 +1344,9 @@ int launch_fields(const SysCall *calls, const Fields *f, int nsys, const Schedul
         if (sh.maxn1 <= 4) {
             if (g8) TAGI_TRY(launch_persistent(far_group<SS, 4, 8>, wf, s, fsm));
             else TAGI_TRY(launch_persistent(far_group<SS, 4, 4>, wf, s, fsm));
-        } else if (sh.maxn1 == 8 && sh.minn1 == 8) {   // degree 7 everywhere: loops known at compile time
-            if (g8) TAGI_TRY(launch_persistent(far_group<SS, 8, 8, true>, wf, s, fsm));
-            else TAGI_TRY(launch_persistent(far_group<SS, 8, 4, true>, wf, s, fsm));
+        } else if (sh.maxn1 == 8 && sh.minn1 == 8) {   // degree 7 everywhere: pipelined staging, fixed loops
+            if (g8) TAGI_TRY(launch_persistent(far_group_db<SS, 8>, wf, s, far_group_db_smem(8)));
+            else TAGI_TRY(launch_persistent(far_group_db<SS, 4>, wf, s, far_group_db_smem(4)));
         } else if (sh.maxn1 <= 8) {
             if (g8) TAGI_TRY(launch_persistent(far_group<SS, 8, 8>, wf, s, fsm));
             else TAGI_TRY(launch_persistent(far_group<SS, 8, 4>, wf, s, fsm));
