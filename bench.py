@@ -21,7 +21,7 @@ one tagi_treecode_dev call per orbital (tree + convolution, leaves 500) --
 timed on orbitals 0 and 31 of the same mesh.
 
   python bench.py [--gpus N] [--steps K] [--warmup W] [--impl gb300|reference]
-                  [--workload orbitals|hartree|uneven|scf|mesh|twomesh]
+                  [--workload orbitals|hartree|uneven|scf|mesh|twomesh|interp]
 
 ``--workload hartree``: one Coulomb Hartree convolution with subtraction on a
 ~1.5M-point mesh (4 nuclei in a 6 Bohr box, 3 Gaussians per nucleus), mixed.
@@ -102,7 +102,7 @@ def parse():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     ap.add_argument("--workload", default="orbitals",
-                    choices=["orbitals", "hartree", "uneven", "scf", "mesh", "twomesh"])
+                    choices=["orbitals", "hartree", "uneven", "scf", "mesh", "twomesh", "interp"])
     ap.add_argument("--scf-points", type=int, default=3_000_000, help="scf workload: mesh points")
     ap.add_argument("--scf-max-iter", type=int, default=60)
     ap.add_argument("--scf-orbitals", type=int, default=21, help="scf workload: orbitals (21 occupied)")
@@ -163,10 +163,10 @@ def make_workload(name):
 # Hardware pipe roofline
 # ---------------------------------------------------------------------------
 def pipe_rates(L, nat, stream):
-    """Lane operations/s of FFMA, FFMA2, MUFU ex2, MUFU rsqrt on this GPU (tagi_pipe_rates)."""
-    r = (ctypes.c_double * 6)()
+    """Lane operations/s of FFMA, FFMA2, MUFU ex2, MUFU rsqrt, DFMA on this GPU (tagi_pipe_rates)."""
+    r = (ctypes.c_double * 7)()
     nat.check(L.tagi_pipe_rates(r, ctypes.c_void_p(stream.cuda_stream)))
-    return dict(ffma=r[0], ffma2=r[1], ex2=r[2], rsqrt=r[3], probe_mhz=r[4], sms=int(r[5]))
+    return dict(ffma=r[0], ffma2=r[1], ex2=r[2], rsqrt=r[3], probe_mhz=r[4], sms=int(r[5]), dfma=r[6])
 
 
 def pipe_roofline(units, ms, ops, rates, clock_mhz):
@@ -444,12 +444,40 @@ def reference_arm_twomesh(args):
             "e2e": {"value": value, "unit": unit, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
 
 
+def reference_arm_interp(args):
+    """The oracle's interpolation (one thread) on every 8th cell of the ring mesh, per step."""
+    from oracle import mesh_oracle as MO
+    pkg = importlib.import_module(PKG)
+    c = MESH_CFG
+    nuclei, _ = pkg.synthetic.ring_molecule()
+    tab, pts = MO.build(c["XL"], c["max_side"], nuclei, c["order"], c["h"], c["H"], c["r"], c["level"])
+    X, Y, Z, W, Xf, Yf, Zf, Wf = pts
+    h = dict(X=X, Y=Y, Z=Z, Xf=Xf, Yf=Yf, Zf=Zf)
+    F = np.zeros(len(X))
+    for R in nuclei:
+        F += np.exp(-np.sqrt((X - R[0]) ** 2 + (Y - R[1]) ** 2 + (Z - R[2]) ** 2))
+    ppc_c, ppc_f = tab["ppc_c"].astype(np.int32), tab["ppc_f"].astype(np.int32)
+    secs, info = [], None
+    for k in range(args.warmup + args.steps):
+        a = time.perf_counter()
+        info = cpu_interp_sample(h, F, ppc_c, ppc_f, c["order"])
+        if k >= args.warmup:
+            secs.append(time.perf_counter() - a)
+    value = info["value"]
+    return {"metric": "two-mesh interpolation, fine points/s", "value": value, "unit": "fine points/s",
+            "ms_per_step": float(np.mean(secs)) * 1e3, "dtype": "f64",
+            "config": {"workload": "ring_two_mesh_interpolation", **c},
+            "cpu_baseline": info,
+            "e2e": {"value": value, "unit": "fine points/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+
+
 def reference_arm(args):
     ws, rank, local = dist_env()
     if rank != 0:
         return 0
-    if args.workload in ("mesh", "twomesh"):
-        body = (reference_arm_mesh if args.workload == "mesh" else reference_arm_twomesh)(args)
+    if args.workload in ("mesh", "twomesh", "interp"):
+        body = {"mesh": reference_arm_mesh, "twomesh": reference_arm_twomesh,
+                "interp": reference_arm_interp}[args.workload](args)
         line = {"impl": "reference", "n_gpus": 0, "steps": args.steps, "warmup": args.warmup,
                 "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
                 "data": "synthetic ring molecule (seeded)", **body}
@@ -1191,6 +1219,137 @@ def mesh_arm(args):
     return 0
 
 
+def interp_arm(args):
+    """Two-mesh interpolation (tagi_interp_dev, the device form of
+    InterpolateBetweenTwoMeshes) of a smooth coarse function -- a sum of
+    Slater functions on the ring molecule's 12 nuclei -- from the ring's coarse
+    mesh (2.61M points, 5,104 cells, order 7) to its fine mesh (14.3M points),
+    the way the two-mesh correction interpolates the density and every orbital.
+    value = fine points interpolated per second, coarse values and both meshes
+    resident in HBM; e2e = the same through the host-pointer drop-in
+    InterpolateBetweenTwoMeshes with every array on the host.  Roofline: the
+    FP64 pipe (three 1-D contractions, 3(p+1) multiply-adds per fine point);
+    the algorithmic bytes (coarseN + 4 fineN) x 8 are reported beside it
+    against the measured HBM rate."""
+    import torch
+    ws, rank, local = dist_env()
+    torch.cuda.set_device(local)
+    if rank != 0:
+        return 0
+    pkg = importlib.import_module(PKG)
+    M = importlib.import_module(PKG + ".mesh")
+    dev = importlib.import_module(PKG + ".device")
+    nat = pkg._native
+    L = nat.lib()
+    c = MESH_CFG
+    nuclei, _ = pkg.synthetic.ring_molecule()
+    order = c["order"]
+    m = M.build_mesh(c["XL"], c["max_side"], nuclei, order, c["h"], c["H"], c["r"], c["level"])
+    F = torch.zeros_like(m.X)
+    for R in nuclei:
+        F += torch.exp(-torch.sqrt((m.X - R[0]) ** 2 + (m.Y - R[1]) ** 2 + (m.Z - R[2]) ** 2))
+    ncells = int(m.PtsPerCellCoarse.numel())
+    nc, nf = int(m.X.numel()), int(m.Xf.numel())
+    out = torch.zeros(nf, dtype=torch.float64, device="cuda")
+    stream = torch.cuda.current_stream()
+
+    def step():
+        out.zero_()
+        dev.interp(m.X, m.Y, m.Z, F, m.PtsPerCellCoarse, m.Xf, m.Yf, m.Zf, m.PtsPerCellFine, ncells, order,
+                   fineF=out)
+
+    for _ in range(max(args.warmup, 3)):
+        step()
+    torch.cuda.synchronize()
+    n0 = L.tagi_launch_count()
+    evs = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(args.steps)]
+    with ClockSampler(local) as clocks:
+        for k in range(args.steps):
+            evs[k][0].record(stream)
+            step()
+            evs[k][1].record(stream)
+        torch.cuda.synchronize()
+    launches = int(L.tagi_launch_count() - n0)
+    ms = float(np.mean([a.elapsed_time(b) for a, b in evs]))
+    clk = clocks.summary()
+    # exactness: the fine function against the same formula evaluated on the fine points
+    Ff = torch.zeros_like(m.Xf)
+    for R in nuclei:
+        Ff += torch.exp(-torch.sqrt((m.Xf - R[0]) ** 2 + (m.Yf - R[1]) ** 2 + (m.Zf - R[2]) ** 2))
+    interp_err = float(torch.linalg.norm(out - Ff) / torch.linalg.norm(Ff))
+    rates = pipe_rates(L, nat, stream)
+    p1 = order + 1
+    # the mesh's fine points lie on tensor grids per child cell, so the kernel takes its
+    # sum-factorised path: three 1-D contractions, 3 (p+1) multiply-adds per fine point
+    # (plus 3 (p+1)^2 divisions per block of (p+1)^3 points, left out of the count)
+    dfma_per_point = 3 * p1
+    ach_fp64 = nf * dfma_per_point / (ms * 1e-3)
+    alg_bytes = 8.0 * (nc + 4 * nf)
+    peaks = {}
+    try:
+        with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as f:
+            peaks = json.load(f)
+    except OSError:
+        pass
+    hbm = peaks.get("hbm_gbs") or 6800.0
+    roof = {"bound": "fp64", "kernel": "interp_cells (one CTA per cell, sum-factorised tensor-grid path)",
+            "achieved": ach_fp64 / 1e9, "peak": rates["dfma"] / 1e9, "unit": "G DFMA/s",
+            "frac": ach_fp64 / rates["dfma"], "ops_per_fine_point": dfma_per_point, "traffic": None,
+            "peak_source": "FP64 DFMA rate measured live on this GPU (tagi_pipe_rates)",
+            "hbm_view": {"algorithmic_bytes": alg_bytes, "achieved_gbs": alg_bytes / (ms * 1e-3) / 1e9,
+                         "peak_gbs": hbm, "frac": alg_bytes / (ms * 1e-3) / 1e9 / hbm,
+                         "peak_source": "measured" if "hbm_gbs" in peaks else "fallback"}}
+    # e2e: the host-pointer drop-in with every array on the host
+    h = {k: getattr(m, k).cpu().numpy() for k in ("X", "Y", "Z", "Xf", "Yf", "Zf")}
+    hF = F.cpu().numpy()
+    hppc_c = m.PtsPerCellCoarse.cpu().numpy().astype(np.int32)
+    hppc_f = m.PtsPerCellFine.cpu().numpy().astype(np.int32)
+    e2e_s = []
+    for _ in range(max(1, min(args.steps, 3))):
+        hout = np.zeros(nf)
+        a = time.perf_counter()
+        nat.lib().InterpolateBetweenTwoMeshes(*[nat.dptr(h[k]) for k in ("X", "Y", "Z")], nat.dptr(hF),
+                                              nat.iptr(hppc_c), nc, *[nat.dptr(h[k]) for k in ("Xf", "Yf", "Zf")],
+                                              nat.dptr(hout), nat.iptr(hppc_f), nf, ncells, order)
+        e2e_s.append(time.perf_counter() - a)
+    line = {"metric": "two-mesh interpolation, fine points/s", "value": nf / (ms * 1e-3), "unit": "fine points/s",
+            "n_gpus": 1, "steps": args.steps, "warmup": max(args.warmup, 3), "ms_per_step": ms,
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+            "data": "synthetic ring molecule (12 nuclei), Slater-sum function",
+            "config": {"workload": "ring_two_mesh_interpolation", **c, "cells": ncells, "coarse_points": nc,
+                       "fine_points": nf, "rel_l2_vs_exact_function": interp_err,
+                       "l2": "inputs and output (~600 MB) larger than L2"},
+            "roofline": roof,
+            "e2e": {"value": nf / float(np.mean(e2e_s)), "unit": "fine points/s",
+                    "h2d_bytes_per_step": int(8 * (4 * nc + 3 * nf) + 8 * ncells),
+                    "d2h_bytes_per_step": int(8 * nf), "path": "InterpolateBetweenTwoMeshes (host pointers)"},
+            "clocks": clk, "gpu_launches": launches}
+    if not args.no_cpu_baseline:
+        line["cpu_baseline"] = cpu_interp_sample(h, hF, hppc_c, hppc_f, order)
+    print(json.dumps(line), flush=True)
+    return 0
+
+
+def cpu_interp_sample(h, hF, ppc_c, ppc_f, order, every=8):
+    """The oracle's restatement of InterpolateBetweenTwoMeshes (single-threaded
+    C, like the reference's own loop over cells) on every `every`-th cell,
+    scaled to all fine points."""
+    from oracle import oracle as O
+    O.build()
+    oc = np.concatenate([[0], np.cumsum(ppc_c)])
+    of = np.concatenate([[0], np.cumsum(ppc_f)])
+    cells = np.arange(0, len(ppc_c), every)
+    ci = np.concatenate([np.arange(oc[k], oc[k + 1]) for k in cells])
+    fi = np.concatenate([np.arange(of[k], of[k + 1]) for k in cells])
+    a = time.perf_counter()
+    O.interp(h["X"][ci], h["Y"][ci], h["Z"][ci], hF[ci], ppc_c[cells], h["Xf"][fi], h["Yf"][fi], h["Zf"][fi],
+             ppc_f[cells], len(cells), order)
+    secs = time.perf_counter() - a
+    return {"value": len(fi) / secs, "unit": "fine points/s", "cores": 1, "kind": "port",
+            "sample": f"oracle restatement of InterpolateBetweenTwoMeshes (one thread, as the reference's C) on "
+                      f"every {every}th cell ({len(cells)} cells, {len(fi)} fine points)"}
+
+
 def cpu_two_mesh_sample(tab, pts, nuclei, target_seconds, threads):
     """Oracle cost of one orbital's two-mesh correction on a mesh: the FP64
     plan (coarse targets, fine sources, theta 0.55, degree 9) and upward pass
@@ -1366,6 +1525,8 @@ def main():
         return mesh_arm(args)
     if args.workload == "twomesh":
         return twomesh_arm(args)
+    if args.workload == "interp":
+        return interp_arm(args)
     if args.workload == "uneven":
         return uneven_arm(args)
     if args.workload == "scf":

@@ -249,8 +249,10 @@ constexpr int PW = 8;  // warps per CTA in mesh_points_warp
 // (ii, jj, kk) of a fine cell.  Every sub-cell holds (order+1)^3 points, so
 // sub-cell s writes points [s p3, (s+1) p3).  Lanes < order+1 evaluate the
 // 1-D nodes x = lo + (hi-lo)/2 (u+1) and scaled weights (hi-lo)/2 W of each
-// axis once (meshUtilities.py:857-883); every point is then three shared
-// loads, w = ((wx_i wy_j) wz_k) and four coalesced stores.
+// axis once (meshUtilities.py:857-883), then the (order+1)^2 products
+// wx_i wy_j; every point is then four shared loads, w = (wx_i wy_j) wz_k
+// (the same two roundings in the same order as the reference's tensor
+// product, one of them shared by a row of points) and four coalesced stores.
 __global__ void __launch_bounds__(PW * 32) mesh_points_warp(const double *__restrict__ cx,
                                                             const double *__restrict__ cy,
                                                             const double *__restrict__ cz,
@@ -264,9 +266,11 @@ __global__ void __launch_bounds__(PW * 32) mesh_points_warp(const double *__rest
                                                             double *__restrict__ X, double *__restrict__ Y,
                                                             double *__restrict__ Z, double *__restrict__ W) {
     __shared__ double sh[PW][6][MESH_MAX_P1];
+    __shared__ double sh_wxy[PW][MESH_MAX_P1 * MESH_MAX_P1];
     const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
     const int p3 = p1 * p1 * p1;
     double(*nd)[MESH_MAX_P1] = sh[wid];
+    double *wxy = sh_wxy[wid];
     for (long s = (long)blockIdx.x * PW + wid; s < nsubcells; s += (long)gridDim.x * PW) {
         int c = (int)s, m = 1, child = 0;
         if (sub_off) {
@@ -295,6 +299,11 @@ __global__ void __launch_bounds__(PW * 32) mesh_points_warp(const double *__rest
             }
         }
         __syncwarp();
+        for (int ij = lane; ij < p1 * p1; ij += 32) {
+            const int i = ij / p1, j = ij - i * p1;
+            wxy[ij] = __dmul_rn(nd[3][i], nd[4][j]);
+        }
+        __syncwarp();
         const long base = s * p3;
         for (int q = lane; q < p3; q += 32) {
             // i = q / p2, j = (q / p1) % p1, k = q % p1 by high multiplies with
@@ -306,7 +315,7 @@ __global__ void __launch_bounds__(PW * 32) mesh_points_warp(const double *__rest
             X[base + q] = nd[0][i];
             Y[base + q] = nd[1][j];
             Z[base + q] = nd[2][k];
-            W[base + q] = __dmul_rn(__dmul_rn(nd[3][i], nd[4][j]), nd[5][k]);
+            W[base + q] = __dmul_rn(wxy[i * p1 + j], nd[5][k]);
         }
         __syncwarp();
     }

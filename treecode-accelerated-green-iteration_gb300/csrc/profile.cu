@@ -47,7 +47,7 @@ void phase_mark(int phase, bool begin, cudaStream_t s) {
 // Hardware pipe rates.  Every thread runs 8 independent dependency chains of
 // one instruction kind, every SM holds 2048 threads, nothing touches memory
 // until the end.  OP 0: FFMA; 1: FFMA2 (packed pair, 2 lanes); 2: MUFU ex2;
-// 3: MUFU rsqrt.  Each block's thread 0 records the clock64 span of its
+// 3: MUFU rsqrt; 4: DFMA (FP64).  Each block's thread 0 records the clock64 span of its
 // block; the longest span over event time is the SM clock during the run.
 // ---------------------------------------------------------------------------
 namespace {
@@ -59,10 +59,12 @@ __global__ void __launch_bounds__(PR_THREADS) pipe_rate_kernel(int reps, float *
     const long long c0 = clock64();
     float a[PR_CHAINS];
     float2 b[PR_CHAINS];
+    double c[PR_CHAINS];
 #pragma unroll
     for (int i = 0; i < PR_CHAINS; i++) {
         a[i] = 0.5f + 1e-3f * (threadIdx.x + i);
         b[i] = make_float2(a[i], a[i] + 0.25f);
+        c[i] = (double)a[i];
     }
     const float2 m2 = make_float2(0.9999f, 0.9998f), c2 = make_float2(1e-4f, 2e-4f);
     for (int r = 0; r < reps; r++) {
@@ -74,12 +76,13 @@ __global__ void __launch_bounds__(PR_THREADS) pipe_rate_kernel(int reps, float *
                 if (OP == 1) b[i] = __ffma2_rn(b[i], m2, c2);
                 if (OP == 2) asm volatile("ex2.approx.ftz.f32 %0, %0;" : "+f"(a[i]));
                 if (OP == 3) asm volatile("rsqrt.approx.ftz.f32 %0, %0;" : "+f"(a[i]));
+                if (OP == 4) c[i] = fma(c[i], 0.9999, 1e-4);
             }
         }
     }
     float acc = 0.f;
 #pragma unroll
-    for (int i = 0; i < PR_CHAINS; i++) acc += a[i] + b[i].x + b[i].y;
+    for (int i = 0; i < PR_CHAINS; i++) acc += a[i] + b[i].x + b[i].y + (float)c[i];
     out[blockIdx.x * PR_THREADS + threadIdx.x] = acc;
     if (threadIdx.x == 0) atomicMax(cycles, (unsigned long long)(clock64() - c0));   // the longest-running block
 }
@@ -134,24 +137,26 @@ int pipe_rates(double *rates, cudaStream_t s) {
     int dev = 0, sms = 0;
     TAGI_CUDA(cudaGetDevice(&dev));
     TAGI_CUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
-    int grid = 0, g[4];
+    int grid = 0, g[5];
     TAGI_TRY(pipe_grid<0>(sms, &g[0]));
     TAGI_TRY(pipe_grid<1>(sms, &g[1]));
     TAGI_TRY(pipe_grid<2>(sms, &g[2]));
     TAGI_TRY(pipe_grid<3>(sms, &g[3]));
-    for (int i = 0; i < 4; i++) grid = g[i] > grid ? g[i] : grid;
+    TAGI_TRY(pipe_grid<4>(sms, &g[4]));
+    for (int i = 0; i < 5; i++) grid = g[i] > grid ? g[i] : grid;
     Arena tmp;
     tmp.stream = s;
     float *out = nullptr;
     unsigned long long *cyc = nullptr;
     int rc = TAGI_OK;
-    double mhz[4] = {0, 0, 0, 0};
+    double mhz[5] = {0, 0, 0, 0, 0};
     do {
         if ((rc = tmp.alloc(&out, (size_t)grid * PR_THREADS)) || (rc = tmp.alloc(&cyc, 1))) break;
         if ((rc = time_pipe<0>(g[0], out, cyc, s, &rates[0], &mhz[0]))) break;
         if ((rc = time_pipe<1>(g[1], out, cyc, s, &rates[1], &mhz[1]))) break;
         if ((rc = time_pipe<2>(g[2], out, cyc, s, &rates[2], &mhz[2]))) break;
         if ((rc = time_pipe<3>(g[3], out, cyc, s, &rates[3], &mhz[3]))) break;
+        if ((rc = time_pipe<4>(g[4], out, cyc, s, &rates[6], &mhz[4]))) break;
     } while (0);
     tmp.release();
     if (rc) return rc;
