@@ -111,3 +111,29 @@ def test_interp_rejects_inconsistent_cells(pkg, native):
     b = np.linspace(0, 1, 54)
     with pytest.raises(native.TagiError):
         interp.callInterpolator(a, a, a, a, np.array([30]), b, b, b, np.array([54]), 1, 2, True)
+
+
+@pytest.mark.parametrize("shuffle", [False, True])
+def test_interp_tensor_and_general_paths_match_oracle(dev, oracle, shuffle):
+    """Fine points on tensor grids per child block take the sum-factorised path;
+    the same points in shuffled order (no tensor structure) take the per-point
+    formula.  Both equal the oracle's restatement of the reference to 1e-13."""
+    from oracle import mesh_oracle as MO
+    pkg = __import__("importlib").import_module("treecode-accelerated-green-iteration_gb300")
+    nuclei, _ = pkg.synthetic.ring_molecule()
+    order = 5
+    tab, pts = MO.build(20.0, 5.0, nuclei, order, 3.0, 5.0, 2.0, -2.0)
+    X, Y, Z, W, Xf, Yf, Zf, Wf = pts
+    F = np.exp(-np.sqrt(X ** 2 + Y ** 2 + Z ** 2) / 3.0) * (1.0 + 0.1 * X)
+    ppc_c, ppc_f = tab["ppc_c"].astype(np.int32), tab["ppc_f"].astype(np.int32)
+    if shuffle:   # permute the fine points inside every cell
+        rng = np.random.default_rng(9)
+        off = np.concatenate([[0], np.cumsum(ppc_f)])
+        perm = np.concatenate([off[c] + rng.permutation(ppc_f[c]) for c in range(len(ppc_f))])
+        Xf, Yf, Zf = Xf[perm], Yf[perm], Zf[perm]
+    ref = oracle.interp(X, Y, Z, F, ppc_c, Xf, Yf, Zf, ppc_f, len(ppc_c), order)
+    t = to_cuda(X, Y, Z, F, Xf, Yf, Zf)
+    pc = torch.as_tensor(ppc_c, device="cuda")
+    pf = torch.as_tensor(ppc_f, device="cuda")
+    out = dev.interp(t[0], t[1], t[2], t[3], pc, t[4], t[5], t[6], pf, len(ppc_c), order).cpu().numpy()
+    assert np.max(np.abs(out - ref)) <= 1e-13 * np.max(np.abs(ref))
