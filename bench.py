@@ -21,10 +21,12 @@ one tagi_treecode_dev call per orbital (tree + convolution, leaves 500) --
 timed on orbitals 0 and 31 of the same mesh.
 
   python bench.py [--gpus N] [--steps K] [--warmup W] [--impl gb300|reference]
-                  [--workload orbitals|hartree|uneven|scf|mesh|twomesh|interp]
+                  [--workload orbitals|hartree|atom|uneven|scf|mesh|twomesh|interp]
 
 ``--workload hartree``: one Coulomb Hartree convolution with subtraction on a
 ~1.5M-point mesh (4 nuclei in a 6 Bohr box, 3 Gaussians per nucleus), mixed.
+``--workload atom``: the CPU-runnable single-atom case (50,112 points, FP64, the Yukawa
+and Coulomb calls), with the CPU restatement timed on the whole step, unsampled.
 ``--workload uneven``: six independent systems (50k .. 2.5M points, 4..64
 orbitals) in one persistent launch per field pass, replayed as a CUDA graph,
 leaf sizes and kernel shape from the autotuner.  ``--workload mesh`` /
@@ -102,7 +104,7 @@ def parse():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     ap.add_argument("--workload", default="orbitals",
-                    choices=["orbitals", "hartree", "uneven", "scf", "mesh", "twomesh", "interp"])
+                    choices=["orbitals", "hartree", "atom", "uneven", "scf", "mesh", "twomesh", "interp"])
     ap.add_argument("--scf-points", type=int, default=3_000_000, help="scf workload: mesh points")
     ap.add_argument("--scf-max-iter", type=int, default=60)
     ap.add_argument("--scf-orbitals", type=int, default=21, help="scf workload: orbitals (21 occupied)")
@@ -475,12 +477,13 @@ def reference_arm(args):
     ws, rank, local = dist_env()
     if rank != 0:
         return 0
-    if args.workload in ("mesh", "twomesh", "interp"):
+    if args.workload in ("mesh", "twomesh", "interp", "atom"):
         body = {"mesh": reference_arm_mesh, "twomesh": reference_arm_twomesh,
-                "interp": reference_arm_interp}[args.workload](args)
+                "interp": reference_arm_interp, "atom": reference_arm_atom}[args.workload](args)
         line = {"impl": "reference", "n_gpus": 0, "steps": args.steps, "warmup": args.warmup,
                 "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
-                "data": "synthetic ring molecule (seeded)", **body}
+                "data": ("synthetic single Z = 4 atom (deterministic mesh)" if args.workload == "atom"
+                         else "synthetic ring molecule (seeded)"), **body}
         print(json.dumps(line), flush=True)
         return 0
     if args.workload in ("scf", "uneven"):
@@ -1219,6 +1222,140 @@ def mesh_arm(args):
     return 0
 
 
+def atom_workload():
+    """BASELINE configs[0]: one Z = 4 nucleus at the origin of [-20, 20]^3, cells of 6^3
+    first-kind points refined while the centre lies within one cell width of the
+    nucleus, depth <= 5 (50,112 points; the literal factor 4 gives 957k points), psi =
+    e^{-r}/sqrt(pi), V = -4/sqrt(r^2 + 0.01): the Yukawa call on f = V psi (k = 1) and the
+    Coulomb call on rho = 2 psi^2 (alpha = 1), both with subtraction, degree 7,
+    theta 0.7, leaves 500, FP64."""
+    pkg = importlib.import_module(PKG)
+    BT = pkg.BaryTreeInterface
+    mesh, f, rho = pkg.synthetic.single_atom(factor=1.0, max_depth=5)
+    return mesh, ((BT.Kernel.YUKAWA, f), (BT.Kernel.COULOMB, rho)), BT.Singularity.SUBTRACTION
+
+
+def atom_arm(args):
+    """Config 1 end to end: per step the two callTreedriver-style FP64 calls (tree and
+    convolution each, as BaryTree does per call) from device-resident inputs; value =
+    convolutions/s; e2e = the same two calls through tagi_BaryTreeInterface_ex with host
+    buffers.  The CPU baseline is the oracle's FP64 treecode on the whole mesh, unsampled."""
+    import torch
+    ws, rank, local = dist_env()
+    torch.cuda.set_device(local)
+    if rank != 0:
+        return 0
+    pkg = importlib.import_module(PKG)
+    dev = importlib.import_module(PKG + ".device")
+    nat = pkg._native
+    L = nat.lib()
+    mesh, calls, SS = atom_workload()
+    t = lambda a: torch.as_tensor(np.ascontiguousarray(a), dtype=torch.float64, device="cuda")
+    x, y, z, w = t(mesh.x), t(mesh.y), t(mesh.z), t(mesh.w)
+    vals = [(kern, t(q)) for kern, q in calls]
+
+    def step(prec="fp64"):
+        return [dev.treecode(x, y, z, q, x, y, z, q, w, kern, [1.0], SS, THETA, DEGREE, PLAIN_LEAF, PLAIN_LEAF,
+                             precision=prec) for kern, q in vals]
+
+    for _ in range(max(args.warmup, 3)):
+        out = step()
+    torch.cuda.synchronize()
+    stream = torch.cuda.current_stream()
+    evs = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(args.steps)]
+    n0 = L.tagi_launch_count()
+    with ClockSampler(local) as clocks:
+        for k in range(args.steps):
+            evs[k][0].record(stream)
+            out = step()
+            evs[k][1].record(stream)
+        torch.cuda.synchronize()
+    launches = int(L.tagi_launch_count() - n0)
+    ms = float(np.mean([a.elapsed_time(b) for a, b in evs]))
+    # the mixed-precision path on the same calls (same tree parameters)
+    step("mixed")
+    torch.cuda.synchronize()
+    a = torch.cuda.Event(enable_timing=True)
+    b = torch.cuda.Event(enable_timing=True)
+    a.record(stream)
+    mixed = step("mixed")
+    b.record(stream)
+    torch.cuda.synchronize()
+    mixed_ms = a.elapsed_time(b)
+    # e2e through the C ABI with host buffers
+    host = {k: np.ascontiguousarray(getattr(mesh, k)) for k in ("x", "y", "z", "w")}
+    kpar = np.array([1.0])
+    e2e_s = []
+    for _ in range(max(1, min(args.steps, 3))):
+        hout = [np.zeros(mesh.n) for _ in calls]
+        t0 = time.perf_counter()
+        for (kern, q), ho in zip(calls, hout):
+            qq = np.ascontiguousarray(q)
+            nat.check(L.tagi_BaryTreeInterface_ex(mesh.n, mesh.n, nat.dptr(host["x"]), nat.dptr(host["y"]),
+                                                  nat.dptr(host["z"]), nat.dptr(qq), nat.dptr(host["x"]),
+                                                  nat.dptr(host["y"]), nat.dptr(host["z"]), nat.dptr(qq),
+                                                  nat.dptr(host["w"]), nat.dptr(ho), int(kern), 1, nat.dptr(kpar),
+                                                  int(SS), 1, 1, THETA, DEGREE, PLAIN_LEAF, PLAIN_LEAF, 1.0, -1.0, 0,
+                                                  nat.PREC_FP64))
+        e2e_s.append(time.perf_counter() - t0)
+    line = {"metric": METRIC, "value": 2.0 / (ms * 1e-3), "unit": UNIT, "n_gpus": 1, "steps": args.steps,
+            "warmup": max(args.warmup, 3), "ms_per_step": ms, "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "f64", "data": "synthetic single Z = 4 atom (deterministic mesh)",
+            "config": {"workload": "single_atom_z4_50k_fp64_yukawa_and_coulomb", "points": int(mesh.n),
+                       "theta": THETA, "degree": DEGREE, "leaf": [PLAIN_LEAF, PLAIN_LEAF], "precision": "fp64",
+                       "step": "two one-shot calls (tree + convolution each): Yukawa k = 1 on f = V psi, Coulomb "
+                               "alpha = 1 on rho = 2 psi^2, both with subtraction",
+                       "l2": "working set below L2 (50k points); no flush"},
+            "mixed_precision_ms_per_step": mixed_ms,
+            "e2e": {"value": 2.0 / float(np.mean(e2e_s)), "unit": UNIT, "h2d_bytes_per_step": int(2 * 9 * 8 * mesh.n),
+                    "d2h_bytes_per_step": int(2 * 8 * mesh.n), "path": "tagi_BaryTreeInterface_ex x 2 (host buffers)"},
+            "clocks": clocks.summary(), "gpu_launches": launches}
+    if not args.no_cpu_baseline:
+        secs, errs = cpu_atom_step(mesh, calls, SS, [o.cpu().numpy() for o in out], [m.cpu().numpy() for m in mixed])
+        line["cpu_baseline"] = {"value": 2.0 / secs, "unit": UNIT, "cores": os.cpu_count() or 1, "kind": "port",
+                                "sample": "the whole step, unsampled: oracle FP64 treecode (plan + convolution) "
+                                          "for both calls"}
+        line["config"]["rel_l2_vs_oracle"] = errs
+    print(json.dumps(line), flush=True)
+    return 0
+
+
+def cpu_atom_step(mesh, calls, SS, gpu64=None, gpu32=None):
+    """Both config-1 calls by the oracle's FP64 treecode, whole mesh; returns
+    (seconds, rel-L2 of the GPU results against it when given)."""
+    from oracle import oracle as O
+    O.build()
+    t0 = time.perf_counter()
+    refs = []
+    for kern, q in calls:
+        plan = O.Plan(mesh.x, mesh.y, mesh.z, mesh.x, mesh.y, mesh.z, mesh.w, THETA, DEGREE, PLAIN_LEAF, PLAIN_LEAF,
+                      1.0)
+        refs.append(plan.convolve(q, q, mesh.w, kern, [1.0], SS, nthreads=os.cpu_count() or 1))
+    secs = time.perf_counter() - t0
+    errs = None
+    if gpu64 is not None:
+        rl = lambda a, r: float(np.linalg.norm(a - r) / np.linalg.norm(r))
+        errs = {"fp64": [rl(a, r) for a, r in zip(gpu64, refs)], "mixed": [rl(a, r) for a, r in zip(gpu32, refs)]}
+    return secs, errs
+
+
+def reference_arm_atom(args):
+    mesh, calls, SS = atom_workload()
+    secs = []
+    for k in range(args.warmup + args.steps):
+        s, _ = cpu_atom_step(mesh, calls, SS)
+        if k >= args.warmup:
+            secs.append(s)
+    value = 2.0 / float(np.mean(secs))
+    return {"metric": METRIC, "value": value, "unit": UNIT, "ms_per_step": float(np.mean(secs)) * 1e3, "dtype": "f64",
+            "config": {"workload": "single_atom_z4_50k_fp64_yukawa_and_coulomb", "points": int(mesh.n),
+                       "theta": THETA, "degree": DEGREE, "leaf": [PLAIN_LEAF, PLAIN_LEAF], "precision": "fp64"},
+            "cpu_baseline": {"value": value, "unit": UNIT, "cores": os.cpu_count() or 1, "kind": "port",
+                             "sample": "the whole step, unsampled: oracle FP64 treecode (plan + convolution) for "
+                                       "both calls"},
+            "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+
+
 def interp_arm(args):
     """Two-mesh interpolation (tagi_interp_dev, the device form of
     InterpolateBetweenTwoMeshes) of a smooth coarse function -- a sum of
@@ -1527,6 +1664,8 @@ def main():
         return twomesh_arm(args)
     if args.workload == "interp":
         return interp_arm(args)
+    if args.workload == "atom":
+        return atom_arm(args)
     if args.workload == "uneven":
         return uneven_arm(args)
     if args.workload == "scf":
