@@ -81,20 +81,27 @@ CPU_SAMPLE_BATCHES = 48  # stratified target batches per CPU-baseline sample
 #               accumulate); Yukawa SS: 6 + (r, 2^-r'/r', q - f_i w, accumulate)
 #   far_mixed   r^2 from per-axis squares (1 + 2/n1 for the row sums), then as
 #               the near loop
-#   near_group  per pair 3 + 3 + r (shared by OG orbitals); per orbital the
-#               split exponent (2), 2^x/r', q - f_i w, accumulate
-#   far_group   per pair r^2 + r (+ 2/n1); per orbital 5
+#   near_group  per pair 3 + 3 + r + (-log2 r) (shared by OG orbitals, one
+#               rsqrt and one lg2); per orbital the split exponent with the
+#               -log2 r folded in (2), q - f_i w, accumulate
+#   far_group   per pair r^2 + r + (-log2 r) (+ 2/n1); per orbital 4
+# Returned as (FP32 lane ops, MUFU ex2, MUFU rsqrt, MUFU lg2) per unit.
 def field_ops(kernel, label, og=8, n1=8):
     yuk = label.startswith("yukawa")
     if kernel == "near_mixed":
-        return (10.0, 1.0, 1.0) if yuk else (9.0, 1.0, 1.0)
+        return (10.0, 1.0, 1.0, 0.0) if yuk else (9.0, 1.0, 1.0, 0.0)
     if kernel == "far_mixed":
-        return (5.0 + 2.0 / n1, 1.0, 1.0) if yuk else (4.0 + 2.0 / n1, 1.0, 1.0)
+        return (5.0 + 2.0 / n1, 1.0, 1.0, 0.0) if yuk else (4.0 + 2.0 / n1, 1.0, 1.0, 0.0)
     if kernel == "near_group":
-        return (5.0 + 7.0 / og, 1.0, 1.0 / og)
+        return (4.0 + 8.0 / og, 1.0, 1.0 / og, 1.0 / og)
     if kernel == "far_group":
-        return (5.0 + (2.0 + 2.0 / n1) / og, 1.0, 1.0 / og)
+        return (4.0 + (3.0 + 2.0 / n1) / og, 1.0, 1.0 / og, 1.0 / og)
     raise ValueError(kernel)
+
+
+def mufu_seconds(ops, rates):
+    """Seconds per unit on the MUFU pipe: ex2, rsqrt and lg2 share it, so their times add."""
+    return ops[1] / rates["ex2"] + ops[2] / rates["rsqrt"] + ops[3] / rates["lg2"]
 
 
 def parse():
@@ -165,22 +172,23 @@ def make_workload(name):
 # Hardware pipe roofline
 # ---------------------------------------------------------------------------
 def pipe_rates(L, nat, stream):
-    """Lane operations/s of FFMA, FFMA2, MUFU ex2, MUFU rsqrt, DFMA on this GPU (tagi_pipe_rates)."""
-    r = (ctypes.c_double * 7)()
+    """Lane operations/s of FFMA, FFMA2, MUFU ex2/rsqrt/lg2, DFMA on this GPU (tagi_pipe_rates)."""
+    r = (ctypes.c_double * 8)()
     nat.check(L.tagi_pipe_rates(r, ctypes.c_void_p(stream.cuda_stream)))
-    return dict(ffma=r[0], ffma2=r[1], ex2=r[2], rsqrt=r[3], probe_mhz=r[4], sms=int(r[5]), dfma=r[6])
+    return dict(ffma=r[0], ffma2=r[1], ex2=r[2], rsqrt=r[3], probe_mhz=r[4], sms=int(r[5]), dfma=r[6],
+                lg2=r[7])
 
 
 def pipe_roofline(units, ms, ops, rates, clock_mhz):
     """Roofline of a field kernel against the FP32 and MUFU pipes.
 
     units: work units of the launch; ms: its duration; ops = (FP32 lane ops,
-    ex2, rsqrt) per unit; rates: measured lane-op rates.  MUFU ex2 and rsqrt
-    share one pipe, so their times add.  Returns the kernel's units/s, the
+    ex2, rsqrt, lg2) per unit; rates: measured lane-op rates.  MUFU ex2, rsqrt
+    and lg2 share one pipe, so their times add.  Returns the kernel's units/s, the
     units/s the binding pipe allows, and each pipe's busy fraction."""
     fp32 = max(rates["ffma"], rates["ffma2"])
     t_fma = ops[0] / fp32
-    t_mufu = ops[1] / rates["ex2"] + ops[2] / rates["rsqrt"]
+    t_mufu = mufu_seconds(ops, rates)
     achieved = units / (ms * 1e-3)
     peak = 1.0 / max(t_fma, t_mufu)
     fr = {"fp32": achieved * t_fma, "mufu": achieved * t_mufu}
@@ -189,10 +197,10 @@ def pipe_roofline(units, ms, ops, rates, clock_mhz):
     if clock_mhz:
         clk = rates["sms"] * clock_mhz * 1e6
         per_clk = {"ffma_lanes": rates["ffma"] / clk, "ffma2_lanes": rates["ffma2"] / clk,
-                   "ex2": rates["ex2"] / clk, "rsqrt": rates["rsqrt"] / clk}
+                   "ex2": rates["ex2"] / clk, "rsqrt": rates["rsqrt"] / clk, "lg2": rates["lg2"] / clk}
     return {"bound": bound, "achieved": achieved, "peak": peak, "frac": achieved / peak,
-            "pipe_frac": fr, "ops_per_unit": {"fp32": ops[0], "ex2": ops[1], "rsqrt": ops[2]},
-            "pipe_rates_lane_ops_per_s": {k: rates[k] for k in ("ffma", "ffma2", "ex2", "rsqrt")},
+            "pipe_frac": fr, "ops_per_unit": {"fp32": ops[0], "ex2": ops[1], "rsqrt": ops[2], "lg2": ops[3]},
+            "pipe_rates_lane_ops_per_s": {k: rates[k] for k in ("ffma", "ffma2", "ex2", "rsqrt", "lg2")},
             "pipe_rates_per_sm_clk": per_clk}
 
 
@@ -935,17 +943,22 @@ def uneven_arm(args):
         torch.cuda.synchronize()
         plain.append(time.perf_counter() - a)
     # pair counts of the plain trees (plan only) to extend the measured FP64 rate to every system
-    plain_pairs = []
-    for mesh in meshes:
-        p = dev.TreecodePlan.for_mesh(*mesh, theta=THETA, degree=DEGREE, source_leaf=PLAIN_LEAF,
-                                      target_leaf=PLAIN_LEAF)
-        inf = p.info()
-        plain_pairs.append(inf["near_pairs"] + inf["far_pairs"])
-        p.close()
-    rate64 = sum(plain_pairs[:len(plain)]) / sum(plain)
-    plain_s = sum(no * (plain[i] if i < len(plain) else plain_pairs[i] / rate64)
-                  for i, no in enumerate(norbs))
-    plain_value = orb_total / plain_s
+    plain_fp64 = None
+    if plain:
+        plain_pairs = []
+        for mesh in meshes:
+            p = dev.TreecodePlan.for_mesh(*mesh, theta=THETA, degree=DEGREE, source_leaf=PLAIN_LEAF,
+                                          target_leaf=PLAIN_LEAF)
+            inf = p.info()
+            plain_pairs.append(inf["near_pairs"] + inf["far_pairs"])
+            p.close()
+        rate64 = sum(plain_pairs[:len(plain)]) / sum(plain)
+        plain_s = sum(no * (plain[i] if i < len(plain) else plain_pairs[i] / rate64)
+                      for i, no in enumerate(norbs))
+        plain_fp64 = {"value": orb_total / plain_s, "unit": "orbital convolutions/s",
+                      "measured_systems": len(plain), "seconds_per_orbital_measured": plain,
+                      "fp64_pairs_per_s": rate64,
+                      "note": "systems beyond the measured ones extrapolated by their plain-tree pair counts"}
 
     # end to end: host arrays -> tagi_treecode_batched (plans, tuned leaves per call) -> host
     off = np.concatenate([[0], np.cumsum(npts)]).astype(np.int32)
@@ -999,11 +1012,8 @@ def uneven_arm(args):
                    "pairs_per_step": pairs_all},
         "phase_ms_uncaptured_call": {k_: float(v_) for k_, v_ in zip(
             ("tree", "lists", "upward", "near", "far", "glue", "near_close"), prof_ms)},
-        "plain_fp64_one_call_per_orbital": {
-            "value": plain_value, "unit": "orbital convolutions/s",
-            "measured_systems": len(plain), "seconds_per_orbital_measured": plain,
-            "fp64_pairs_per_s": rate64, "speedup_of_batched": value / plain_value,
-            "note": "systems beyond the measured ones extrapolated by their plain-tree pair counts"},
+        "plain_fp64_one_call_per_orbital": (dict(plain_fp64, speedup_of_batched=value / plain_fp64["value"])
+                                            if plain_fp64 else None),
         "roofline": roofline, "roofline_other": roofs[names[1] if dom == names[0] else names[0]],
         "cpu_baseline": cpu, "e2e": e2e, "clocks": clk,
         "gpu_launches": launches_per_replay * args.steps,
@@ -1592,7 +1602,7 @@ def twomesh_arm(args):
              (21 * pairs1, field_ops(f"{dominant}_group", "yukawa_ss", 8, n1)))
     fp32 = max(rates["ffma"], rates["ffma2"])
     t_fma = sum(u * o[0] for u, o in mixes) / fp32
-    t_mufu = sum(u * (o[1] / rates["ex2"] + o[2] / rates["rsqrt"]) for u, o in mixes)
+    t_mufu = sum(u * mufu_seconds(o, rates) for u, o in mixes)
     bound_ms = max(t_fma, t_mufu) * 1e3
     achieved = (22 * pairs1) / (k_ms * 1e-3)
     # e2e: host orbitals and density in, corrected eigenvalues out

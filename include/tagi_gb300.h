@@ -441,7 +441,7 @@ int tagi_pair_peak(int kernel, int singularity, int variant, double kernelParame
  * packed FFMA2 (two lanes per instruction), rates[2] MUFU ex2, rates[3]
  * MUFU rsqrt, rates[4] the SM clock in MHz seen during the FFMA run (clock64
  * cycles over CUDA-event time), rates[5] the number of SMs, rates[6] FP64
- * DFMA.  rates must hold 7 values.  The field kernels' roofline is their
+ * DFMA, rates[7] MUFU lg2.  rates must hold 8 values.  The field kernels' roofline is their
  * arithmetic per pair against these rates. */
 int tagi_pipe_rates(double *rates, void *stream);
 int tagi_profile(int enable);

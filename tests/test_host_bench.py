@@ -18,28 +18,32 @@ def bench():
     return importlib.import_module("bench")
 
 
-RATES = dict(ffma=3.86e13, ffma2=3.72e13, ex2=1.0e13, rsqrt=5.0e12, sms=152)
+RATES = dict(ffma=3.86e13, ffma2=3.72e13, ex2=1.0e13, rsqrt=5.0e12, lg2=5.0e12, sms=152)
 
 
 def test_pipe_roofline_picks_the_binding_pipe(bench):
     # Coulomb near: 9 FP32 lane ops, 1 ex2, 1 rsqrt per pair -> MUFU-bound
-    r = bench.pipe_roofline(1e12, 500.0, (9.0, 1.0, 1.0), RATES, 2070.0)
+    r = bench.pipe_roofline(1e12, 500.0, (9.0, 1.0, 1.0, 0.0), RATES, 2070.0)
     t_mufu = 1 / 1.0e13 + 1 / 5.0e12
     assert r["bound"] == "mufu"
     assert abs(r["peak"] - 1 / t_mufu) / r["peak"] < 1e-12
     assert abs(r["frac"] - 2e12 * t_mufu) < 1e-12
     assert abs(r["pipe_frac"]["fp32"] - 2e12 * 9 / 3.86e13) < 1e-12
-    # the orbital-group loop: FP32-bound
-    g = bench.pipe_roofline(1e12, 500.0, bench.field_ops("near_group", "yukawa_ss", 8, 8), RATES, None)
-    assert g["bound"] == "fp32" and g["pipe_rates_per_sm_clk"] is None
+    # the orbital-group loop: ex2 per pair-orbital, rsqrt and lg2 per pair on MUFU
+    ops = bench.field_ops("near_group", "yukawa_ss", 8, 8)
+    g = bench.pipe_roofline(1e12, 500.0, ops, RATES, None)
+    t_m = 1 / 1.0e13 + 0.125 / 5.0e12 + 0.125 / 5.0e12
+    t_f = 5.0 / 3.86e13
+    assert g["bound"] == ("mufu" if t_m > t_f else "fp32") and g["pipe_rates_per_sm_clk"] is None
+    assert abs(g["peak"] - 1 / max(t_m, t_f)) / g["peak"] < 1e-12
     assert abs(g["frac"] - g["achieved"] / g["peak"]) < 1e-12
 
 
 def test_field_ops_counts(bench):
-    assert bench.field_ops("near_mixed", "coulomb_ss") == (9.0, 1.0, 1.0)
-    assert bench.field_ops("near_mixed", "yukawa_ss") == (10.0, 1.0, 1.0)
-    assert bench.field_ops("near_group", "yukawa_ss", 8) == (5.875, 1.0, 0.125)
-    assert bench.field_ops("far_group", "yukawa_ss", 8, 8) == (5.28125, 1.0, 0.125)
+    assert bench.field_ops("near_mixed", "coulomb_ss") == (9.0, 1.0, 1.0, 0.0)
+    assert bench.field_ops("near_mixed", "yukawa_ss") == (10.0, 1.0, 1.0, 0.0)
+    assert bench.field_ops("near_group", "yukawa_ss", 8) == (5.0, 1.0, 0.125, 0.125)
+    assert bench.field_ops("far_group", "yukawa_ss", 8, 8) == (4.40625, 1.0, 0.125, 0.125)
     with pytest.raises(ValueError):
         bench.field_ops("nothing", "yukawa_ss")
 

@@ -166,16 +166,24 @@ int plan_create(Plan **out, int nt, const double *tx, const double *ty, const do
         cudaMemsetAsync(p->err_flag, 0, 2 * sizeof(int), s);
         phase_mark(PH_TREE, true, s);
         if ((rc = build_tree(p->src, sx, sy, sz, ns, sl, p->arena, p->err_flag, s))) break;
-        if ((rc = build_tree(p->tgt, tx, ty, tz, nt, tl, p->arena, p->err_flag, s))) break;
+        // Green iteration convolves a mesh with itself: same points and leaf size give the
+        // same (deterministic) tree, so the target tree shares the source tree's arrays
+        const bool same = tx == sx && ty == sy && tz == sz && nt == ns && tl == sl;
+        if (same) p->tgt = p->src;
+        else if ((rc = build_tree(p->tgt, tx, ty, tz, nt, tl, p->arena, p->err_flag, s))) break;
         phase_mark(PH_TREE, false, s);
         phase_mark(PH_LISTS, true, s);
         if ((rc = p->arena.alloc(&p->sw64, ns)) || (rc = p->arena.alloc(&p->sw32, ns))) break;
         launch(gather_weights, (ns + 255) / 256, 256, 0, s, sw, p->src.perm, ns, p->sw64, p->sw32);
-        if ((rc = p->arena.alloc(&p->src_hi, ns)) || (rc = p->arena.alloc(&p->src_lo, ns)) ||
-            (rc = p->arena.alloc(&p->tgt_hi, nt)) || (rc = p->arena.alloc(&p->tgt_lo, nt)))
-            break;
+        if ((rc = p->arena.alloc(&p->src_hi, ns)) || (rc = p->arena.alloc(&p->src_lo, ns))) break;
         launch(split_points, (ns + 255) / 256, 256, 0, s, p->src.x, p->src.y, p->src.z, ns, p->src_hi, p->src_lo);
-        launch(split_points, (nt + 255) / 256, 256, 0, s, p->tgt.x, p->tgt.y, p->tgt.z, nt, p->tgt_hi, p->tgt_lo);
+        if (same) {
+            p->tgt_hi = p->src_hi;
+            p->tgt_lo = p->src_lo;
+        } else {
+            if ((rc = p->arena.alloc(&p->tgt_hi, nt)) || (rc = p->arena.alloc(&p->tgt_lo, nt))) break;
+            launch(split_points, (nt + 255) / 256, 256, 0, s, p->tgt.x, p->tgt.y, p->tgt.z, nt, p->tgt_hi, p->tgt_lo);
+        }
         if ((rc = build_lists(*p, s))) break;
         if ((rc = build_weight_charges(*p, s))) break;
         phase_mark(PH_LISTS, false, s);

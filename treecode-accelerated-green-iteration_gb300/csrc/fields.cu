@@ -53,6 +53,11 @@ __device__ __forceinline__ float ex2_mufu(float x) {
     asm("ex2.approx.ftz.f32 %0, %1;" : "=f"(y) : "f"(x));
     return y;
 }
+__device__ __forceinline__ float lg2_mufu(float x) {
+    float y;
+    asm("lg2.approx.ftz.f32 %0, %1;" : "=f"(y) : "f"(x));
+    return y;
+}
 
 struct Fields {
     // target side (sorted order)
@@ -119,6 +124,10 @@ __device__ __forceinline__ float2 rsqrt2(float2 a) { return make_float2(rsqrt_mu
 __device__ __forceinline__ float2 ex2neg2(float2 a) { return make_float2(ex2_mufu(-a.x), ex2_mufu(-a.y)); }
 // 2^{a} per lane
 __device__ __forceinline__ float2 ex2pos2(float2 a) { return make_float2(ex2_mufu(a.x), ex2_mufu(a.y)); }
+// -log2(r) = -log2(r^2) / 2 per lane
+__device__ __forceinline__ float2 nlog2r2(float2 r2) {
+    return mul2(dup2(-0.5f), make_float2(lg2_mufu(r2.x), lg2_mufu(r2.y)));
+}
 
 // Two pairs (one target, two sources) from their squared scaled distances
 // r2 = r'^2; q, w the two sources' charges and weights, nfi = -f_i in both
@@ -503,9 +512,10 @@ __global__ void __launch_bounds__(FT, 2) far_mixed(const __grid_constant__ Work 
 // ---------------------------------------------------------------------------
 // Orbital-group kernels (Yukawa, mixed precision): one item = (batch, group of
 // OG orbitals).  Per two sources (or two proxy points) the differences, r^2,
-// rsqrt and r are formed once for the group in packed operations; each orbital
-// then adds exp2(-k_o log2(e) r) * rinv * c with its own k (the constant
-// split hi + lo).  Coordinates are translated to the batch center but not
+// r (via rsqrt) and -log2 r (via lg2) are formed once for the group in packed
+// operations; each orbital then adds 2^{-k_o log2(e) r - log2 r} * c, which is
+// e^{-k_o r} / r * c with the 1/r folded into the exponent (the constant
+// -k_o log2(e) split hi + lo).  Coordinates are translated to the batch center but not
 // scaled (each orbital has its own k).  Charges are staged as float4
 // {q(o, j), q(o, j+1), q(o+1, j), q(o+1, j+1)} per (pair of sources, pair of
 // orbitals), so one 16-byte shared read serves four (pair, orbital) terms.
@@ -541,9 +551,12 @@ __device__ __forceinline__ void group_tile(const float (*__restrict__ s)[GTILE],
             const float2 wv = lds2(s[3] + j);
             const float2 r2 = fma2(dx, dx, fma2(dy, dy, mul2(dz, dz)));
             float2 rinv = rsqrt2(r2);
-            if (MASK) {
+            float2 nl = nlog2r2(r2);
+            if (MASK) {   // r = 0: r = 0 and 2^{-inf} = 0, so the pair adds exactly 0
                 rinv.x = r2.x > 0.f ? rinv.x : 0.f;
                 rinv.y = r2.y > 0.f ? rinv.y : 0.f;
+                nl.x = r2.x > 0.f ? nl.x : -INFINITY;
+                nl.y = r2.y > 0.f ? nl.y : -INFINITY;
             }
             const float2 r = mul2(r2, rinv);
 #pragma unroll
@@ -553,8 +566,8 @@ __device__ __forceinline__ void group_tile(const float (*__restrict__ s)[GTILE],
                 for (int u = 0; u < 2; u++) {
                     const int o = 2 * o2 + u;
                     const float2 q = u ? make_float2(q4.z, q4.w) : make_float2(q4.x, q4.y);
-                    // exponent -k log2(e) r with the constant split hi + lo
-                    const float2 g = mul2(ex2pos2(fma2(kc[o], r, mul2(kl[o], r))), rinv);
+                    // e^{-k r} / r = 2^{-k log2(e) r - log2 r}, the constant split hi + lo
+                    const float2 g = ex2pos2(fma2(kc[o], r, fma2(kl[o], r, nl)));
                     part[o] = fma2(g, SS ? fma2(nfi[o], wv, q) : q, part[o]);
                 }
             }
@@ -705,8 +718,8 @@ __device__ __forceinline__ void far_group_cluster(const float4 *__restrict__ s_q
             for (int m = 0; m < MH; m++) {
                 if (2 * m < n1) {
                     const float2 r2 = add2(rxy, dz2[m]);
-                    const float2 rinv = rsqrt2(r2);
-                    const float2 rr = mul2(r2, rinv);
+                    const float2 rr = mul2(r2, rsqrt2(r2));
+                    const float2 nl = nlog2r2(r2);
                     const float2 wk = lds2(s_w + idx + 2 * m);
 #pragma unroll
                     for (int o2 = 0; o2 < OG / 2; o2++) {
@@ -715,7 +728,7 @@ __device__ __forceinline__ void far_group_cluster(const float4 *__restrict__ s_q
                         for (int u = 0; u < 2; u++) {
                             const int o = 2 * o2 + u;
                             const float2 q = u ? make_float2(q4.z, q4.w) : make_float2(q4.x, q4.y);
-                            const float2 g = mul2(ex2pos2(fma2(kc[o], rr, mul2(kl[o], rr))), rinv);
+                            const float2 g = ex2pos2(fma2(kc[o], rr, fma2(kl[o], rr, nl)));
                             part[o] = fma2(g, SS ? fma2(nfi[o], wk, q) : q, part[o]);
                         }
                     }

@@ -47,7 +47,9 @@ void phase_mark(int phase, bool begin, cudaStream_t s) {
 // Hardware pipe rates.  Every thread runs 8 independent dependency chains of
 // one instruction kind, every SM holds 2048 threads, nothing touches memory
 // until the end.  OP 0: FFMA; 1: FFMA2 (packed pair, 2 lanes); 2: MUFU ex2;
-// 3: MUFU rsqrt; 4: DFMA (FP64).  Each block's thread 0 records the clock64 span of its
+// 3: MUFU rsqrt; 4: DFMA (FP64); 5: MUFU lg2.  The ex2 and lg2 chains leave
+// the finite range after a few steps (inf, NaN); the MUFU pipe's rate does not
+// depend on the operand.  Each block's thread 0 records the clock64 span of its
 // block; the longest span over event time is the SM clock during the run.
 // ---------------------------------------------------------------------------
 namespace {
@@ -77,6 +79,7 @@ __global__ void __launch_bounds__(PR_THREADS) pipe_rate_kernel(int reps, float *
                 if (OP == 2) asm volatile("ex2.approx.ftz.f32 %0, %0;" : "+f"(a[i]));
                 if (OP == 3) asm volatile("rsqrt.approx.ftz.f32 %0, %0;" : "+f"(a[i]));
                 if (OP == 4) c[i] = fma(c[i], 0.9999, 1e-4);
+                if (OP == 5) asm volatile("lg2.approx.ftz.f32 %0, %0;" : "+f"(a[i]));
             }
         }
     }
@@ -137,19 +140,20 @@ int pipe_rates(double *rates, cudaStream_t s) {
     int dev = 0, sms = 0;
     TAGI_CUDA(cudaGetDevice(&dev));
     TAGI_CUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
-    int grid = 0, g[5];
+    int grid = 0, g[6];
     TAGI_TRY(pipe_grid<0>(sms, &g[0]));
     TAGI_TRY(pipe_grid<1>(sms, &g[1]));
     TAGI_TRY(pipe_grid<2>(sms, &g[2]));
     TAGI_TRY(pipe_grid<3>(sms, &g[3]));
     TAGI_TRY(pipe_grid<4>(sms, &g[4]));
-    for (int i = 0; i < 5; i++) grid = g[i] > grid ? g[i] : grid;
+    TAGI_TRY(pipe_grid<5>(sms, &g[5]));
+    for (int i = 0; i < 6; i++) grid = g[i] > grid ? g[i] : grid;
     Arena tmp;
     tmp.stream = s;
     float *out = nullptr;
     unsigned long long *cyc = nullptr;
     int rc = TAGI_OK;
-    double mhz[5] = {0, 0, 0, 0, 0};
+    double mhz[6] = {0, 0, 0, 0, 0, 0};
     do {
         if ((rc = tmp.alloc(&out, (size_t)grid * PR_THREADS)) || (rc = tmp.alloc(&cyc, 1))) break;
         if ((rc = time_pipe<0>(g[0], out, cyc, s, &rates[0], &mhz[0]))) break;
@@ -157,6 +161,7 @@ int pipe_rates(double *rates, cudaStream_t s) {
         if ((rc = time_pipe<2>(g[2], out, cyc, s, &rates[2], &mhz[2]))) break;
         if ((rc = time_pipe<3>(g[3], out, cyc, s, &rates[3], &mhz[3]))) break;
         if ((rc = time_pipe<4>(g[4], out, cyc, s, &rates[6], &mhz[4]))) break;
+        if ((rc = time_pipe<5>(g[5], out, cyc, s, &rates[7], &mhz[5]))) break;
     } while (0);
     tmp.release();
     if (rc) return rc;
