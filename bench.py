@@ -99,6 +99,12 @@ def field_ops(kernel, label, og=8, n1=8):
     raise ValueError(kernel)
 
 
+def loop_variant(kernel, og):
+    """tagi_pair_peak variant of a field kernel's inner loop (groups of 16 orbitals: 4, 5)."""
+    base = {"near_mixed": 0, "far_mixed": 1, "near_group": 2, "far_group": 3}[kernel]
+    return base + 2 if og == 16 and base >= 2 else base
+
+
 def mufu_seconds(ops, rates):
     """Seconds per unit on the MUFU pipe: ex2, rsqrt and lg2 share it, so their times add."""
     return ops[1] / rates["ex2"] + ops[2] / rates["rsqrt"] + ops[3] / rates["lg2"]
@@ -645,7 +651,9 @@ def gb300_arm(args):
     del out
 
     # roofline: the dominant field kernel against the hardware pipes
-    og = 8 if (norb >= 8 and wl["label"].startswith("yukawa")) else (4 if norb >= 4 and wl["label"].startswith("yukawa") else 1)
+    og_c = ctypes.c_int()
+    nat.check(L.tagi_orbitals_per_item(int(K), nat.PREC_MIXED, norb, 0, DEGREE, ctypes.byref(og_c)))
+    og = og_c.value
     names = ("near_group", "far_group") if og > 1 else ("near_mixed", "far_mixed")
     units = {names[0]: (info["near_pairs"] - info["near_close_pairs"]) * norb, names[1]: info["far_pairs"] * norb}
     kms = {names[0]: prof_ms[3] / max(prof_n[3], 1), names[1]: prof_ms[4] / max(prof_n[4], 1)}
@@ -654,7 +662,7 @@ def gb300_arm(args):
     for kname in names:
         r = pipe_roofline(units[kname], kms[kname], field_ops(kname, wl["label"], og, DEGREE + 1), rates,
                           clk.get("sm_mhz"))
-        variant = {"near_mixed": 0, "far_mixed": 1, "near_group": 2, "far_group": 3}[kname]
+        variant = loop_variant(kname, og)
         lp = ctypes.c_double()
         nat.check(L.tagi_pair_peak(int(K), int(SS), variant, float(kp[0][0]), ctypes.byref(lp),
                                    ctypes.c_void_p(stream.cuda_stream)))
@@ -916,7 +924,7 @@ def uneven_arm(args):
     for kname, units, kms in ((names[0], pairs_near, near_ms), (names[1], pairs_far, far_ms)):
         r = pipe_roofline(units, kms, field_ops(kname, "yukawa_ss", og, n1max), rates, None)
         lp = ctypes.c_double()
-        variant = {"near_mixed": 0, "far_mixed": 1, "near_group": 2, "far_group": 3}[kname]
+        variant = loop_variant(kname, og)
         nat.check(L.tagi_pair_peak(int(K), int(SS), variant, 1.0, ctypes.byref(lp),
                                    ctypes.c_void_p(stream0.cuda_stream)))
         r.update({"kernel": f"{kname} over all systems" + (f" ({og} orbitals per item)" if og > 1 else ""),

@@ -148,8 +148,8 @@ int tagi_plan_convolve(tagi_plan *plan, int numOrbitals, const double *targetVal
  * (k_i = sqrt(-2 eps_i)) change between replays; such values are not checked
  * on the host: an unusable one (not finite, or <= 0 where the kernel uses it)
  * gives NaN output and sets a flag that tagi_plan_check_parameters returns.
- * orbitalsPerItem: 0 = automatic, 1, 4 or 8 (Yukawa mixed precision shares
- * each pair's geometry across a group of orbitals; other cases use 1).
+ * orbitalsPerItem: 0 = automatic, 1, 4, 8 or 16 (Yukawa mixed precision
+ * shares each pair's geometry across a group of orbitals; other cases use 1).
  * targetsPerThread: 0 = automatic (2 when a batch exceeds 256 targets), 1 or
  * 2 (mixed single-orbital field kernels; a tuning knob, results unchanged).
  * Extends callTreedriver (BaryTreeInterface.py:88-158), which has neither. */
@@ -420,6 +420,11 @@ int tagi_get_precision(void);
 /* beta in [0, 1] -> theta, degree, leaf sizes (project-defined). */
 int tagi_beta_parameters(double beta, double *theta, int *degree, int *sourceLeafSize,
                          int *targetLeafSize);
+/* Orbitals per work item that a convolution of maxOrbitals orbitals at this
+ * degree runs with (requested 0 = automatic, else 1, 4, 8 or 16; the rule of
+ * tagi_plan_convolve_ex and tagi_systems_create). */
+int tagi_orbitals_per_item(int kernel, int precision, int maxOrbitals, int requested, int degree,
+                           int *orbitalsPerItem);
 /* Instrumentation: number of kernels this library has launched in this
  * process; optional per-phase device timing with CUDA events on the
  * launching stream.  Phases: 0 tree, 1 lists, 2 upward pass, 3 near field,
@@ -430,8 +435,9 @@ long long tagi_launch_count(void);
 /* Pair-throughput ceiling of the mixed-precision field kernels' inner loops
  * on this GPU: their arithmetic (variant 0: near-field loop, 1: far-field
  * proxy-grid loop, 2: Yukawa orbital-group near loop and 3: Yukawa
- * orbital-group far loop, 8 orbitals per pair geometry, counted per pair and
- * orbital) with operands in shared memory and registers and no global-memory
+ * orbital-group far loop, 8 orbitals per pair geometry, 4 and 5: the same
+ * with 16 orbitals packed by orbital; groups counted per pair and orbital)
+ * with operands in shared memory and registers and no global-memory
  * traffic, timed with CUDA events.  Pair interactions / s.  A field kernel's
  * rate over this is its loop efficiency, not a hardware roofline. */
 int tagi_pair_peak(int kernel, int singularity, int variant, double kernelParameter,

@@ -58,6 +58,24 @@ def test_host_only_entry_points(native):
     assert L.tagi_last_error() == 0
 
 
+def test_orbital_group_choice(native):
+    """Automatic orbitals per item: 16 when its padded slots cost less than 8's, up to degree 7."""
+    L = native.lib()
+    og = ctypes.c_int()
+
+    def choose(norb, degree=7, requested=0, kernel=2, precision=native.PREC_MIXED):
+        native.check(L.tagi_orbitals_per_item(kernel, precision, norb, requested, degree, ctypes.byref(og)))
+        return og.value
+
+    assert choose(32) == 16 and choose(16) == 16 and choose(28) == 16
+    assert choose(21) == 8 and choose(17) == 8 and choose(24) == 8   # 16-slots padding costs more
+    assert choose(32, degree=9) == 8 and choose(5) == 4 and choose(3) == 1
+    assert choose(32, requested=8) == 8 and choose(3, requested=16) == 16
+    assert choose(32, precision=native.PREC_FP64) == 1 and choose(32, kernel=1) == 1
+    assert L.tagi_orbitals_per_item(2, 0, 32, 12, 7, ctypes.byref(og)) == native.TAGI_ERR_ARG
+    L.tagi_clear_error()
+
+
 def test_argument_errors_before_any_device_work(native):
     """Unsupported options are refused on the host with a status, never exit()."""
     L = native.lib()

@@ -92,6 +92,7 @@ SIGNATURES = {
     "tagi_set_precision": (_i, [_i]),
     "tagi_get_precision": (_i, []),
     "tagi_beta_parameters": (_i, [_d, _dp, _ip, _ip, _ip]),
+    "tagi_orbitals_per_item": (_i, [_i, _i, _i, _i, _i, _ip]),
     "tagi_launch_count": (ctypes.c_longlong, []),
     "tagi_pair_peak": (_i, [_i, _i, _i, _d, _dp, _vp]),
     "tagi_pipe_rates": (_i, [_dp, _vp]),

@@ -6,7 +6,7 @@ target.  The knobs:
 
   * source / target leaf sizes of the plan -- the tree shape sets the
     near/far balance and the target-batch sizes;
-  * orbitals per work item (1, 4 or 8; Yukawa in mixed precision shares each
+  * orbitals per work item (1, 4, 8 or 16; Yukawa in mixed precision shares each
     pair's geometry across a group of orbitals);
   * targets per thread in the single-orbital field kernels (1 or 2).
 
@@ -74,7 +74,7 @@ def _store(path, cache):
 def _group_candidates(kernel, precision, norb):
     if int(kernel) != int(Kernel.YUKAWA) or precision != "mixed":
         return (1,)
-    return tuple(g for g in (1, 4, 8) if g == 1 or norb >= g)
+    return tuple(g for g in (1, 4, 8, 16) if g == 1 or norb >= g)
 
 
 def tune(x, y, z, w, values, kernel, kernel_params, singularity, precision="mixed", theta=0.7,

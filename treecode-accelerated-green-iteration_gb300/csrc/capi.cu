@@ -325,6 +325,16 @@ int tagi_beta_parameters(double beta, double *theta, int *degree, int *sl, int *
     return TAGI_OK;
 }
 
+int tagi_orbitals_per_item(int kernel, int precision, int maxOrbitals, int requested, int degree, int *og) {
+    if (!og) return set_error(TAGI_ERR_ARG, "null pointer");
+    if (requested != 0 && requested != 1 && requested != 4 && requested != 8 && requested != 16)
+        return set_error(TAGI_ERR_ARG, "orbitalsPerItem %d must be 0 (automatic), 1, 4, 8 or 16", requested);
+    if (maxOrbitals < 1 || degree < 1 || degree > MAX_DEGREE)
+        return set_error(TAGI_ERR_ARG, "maxOrbitals %d, degree %d", maxOrbitals, degree);
+    *og = orbitals_per_item(kernel, precision, maxOrbitals, requested, degree + 1);
+    return TAGI_OK;
+}
+
 int tagi_BaryTreeInterface_ex(int numTargets, int numSources, const double *targetX,
                               const double *targetY, const double *targetZ, const double *targetValue,
                               const double *sourceX, const double *sourceY, const double *sourceZ,
@@ -502,9 +512,10 @@ int tagi_pair_peak(int kernel, int singularity, int variant, double kernelParame
                    void *stream) {
     if (!pairsPerSecond) return set_error(TAGI_ERR_ARG, "null output");
     if (kernel != KERNEL_COULOMB && kernel != KERNEL_YUKAWA) return set_error(TAGI_ERR_UNSUPPORTED, "kernel %d", kernel);
-    if (variant < 0 || variant > 3)
+    if (variant < 0 || variant > 5)
         return set_error(TAGI_ERR_ARG,
-                         "variant must be 0 (near), 1 (far), 2 (near, orbital groups) or 3 (far, orbital groups)");
+                         "variant must be 0 (near), 1 (far), 2/3 (near/far, groups of 8 orbitals) or 4/5 "
+                         "(near/far, groups of 16)");
     return pair_peak(kernel, singularity, variant, kernelParameter, pairsPerSecond, (cudaStream_t)stream);
 }
 

@@ -933,6 +933,370 @@ __global__ void __launch_bounds__(FT, 2) far_group_db(const __grid_constant__ Wo
 }
 
 // ---------------------------------------------------------------------------
+// Orbital-group kernels with 16 orbitals per item, packed by ORBITAL: the two
+// lanes of every packed operation are orbitals (2p, 2p+1) of one source (or
+// proxy point).  The per-orbital constants -k log2(e) (hi, lo) and -f_i are
+// then natural float2 pairs -- 8 pairs of registers each for 16 orbitals,
+// where the source-packed layout needs 16 duplicated pairs -- and only the
+// source's r, -log2 r and weight are duplicated, once per source for all 16
+// orbitals.  The geometry (differences, r^2, rsqrt, lg2) of two sources is
+// still formed in packed operations and is shared by 16 orbitals: MUFU work
+// per pair-orbital is 1 ex2 + (rsqrt + lg2)/16.
+// Charges are staged orbital-fastest, QS16 floats per source (16 used + 4 of
+// padding, which spreads the staging writes over all banks); a thread reads
+// one source's 16 charges as four float4.  Each lane sums KCHUNK16 sources of
+// one orbital before the Kahan step, the same run length per lane as the
+// source-packed kernels.
+// ---------------------------------------------------------------------------
+constexpr int QS16 = 20;
+constexpr int KCHUNK16 = 32;
+
+template <bool SS, bool MASK, bool PRECISE>
+__device__ __forceinline__ void group16_tile(const float (*__restrict__ s)[GTILE], const float *__restrict__ s_q,
+                                             int cnt2, float2 tx, float2 ty, float2 tz, float2 lx, float2 ly,
+                                             float2 lz, const float2 (&nfi)[8], const float2 (&kc)[8],
+                                             const float2 (&kl)[8], float (&sum)[16], float (&cmp)[16]) {
+    // r, -log2 r and w of the source pair at j (packed over the two sources)
+    auto geometry = [&](int j, float2 &r, float2 &nl, float2 &wv) {
+        float2 dx = add2(tx, lds2(s[0] + j)), dy = add2(ty, lds2(s[1] + j)), dz = add2(tz, lds2(s[2] + j));
+        if constexpr (PRECISE) {
+            dx = add2(dx, add2(lx, lds2(s[4] + j)));
+            dy = add2(dy, add2(ly, lds2(s[5] + j)));
+            dz = add2(dz, add2(lz, lds2(s[6] + j)));
+        }
+        wv = lds2(s[3] + j);
+        const float2 r2 = fma2(dx, dx, fma2(dy, dy, mul2(dz, dz)));
+        float2 rinv = rsqrt2(r2);
+        nl = nlog2r2(r2);
+        if (MASK) {   // r = 0: r = 0 and 2^{-inf} = 0, so the pair adds exactly 0
+            rinv.x = r2.x > 0.f ? rinv.x : 0.f;
+            rinv.y = r2.y > 0.f ? rinv.y : 0.f;
+            nl.x = r2.x > 0.f ? nl.x : -INFINITY;
+            nl.y = r2.y > 0.f ? nl.y : -INFINITY;
+        }
+        r = mul2(r2, rinv);
+    };
+    float2 part[8];
+#pragma unroll
+    for (int p = 0; p < 8; p++) part[p] = make_float2(0.f, 0.f);
+    // software pipelined: the next pair's geometry (loads, rsqrt, lg2) is
+    // issued before this pair's 16-orbital work, which hides its latency
+    float2 rc, nc, wc;
+    geometry(0, rc, nc, wc);
+#pragma unroll 1
+    for (int j = 0; j < cnt2; j += 2) {
+        float2 rn, nn, wn;
+        geometry(j + 2 < cnt2 ? j + 2 : j, rn, nn, wn);
+#pragma unroll
+        for (int u = 0; u < 2; u++) {
+            const float2 rd = dup2(u ? rc.y : rc.x), nd = dup2(u ? nc.y : nc.x), wd = dup2(u ? wc.y : wc.x);
+            const float *qj = s_q + (j + u) * QS16;
+#pragma unroll
+            for (int o4 = 0; o4 < 4; o4++) {
+                const float4 q4 = lds4(qj + 4 * o4);
+#pragma unroll
+                for (int h = 0; h < 2; h++) {
+                    const int p = 2 * o4 + h;   // orbitals 2p, 2p+1
+                    const float2 q = h ? make_float2(q4.z, q4.w) : make_float2(q4.x, q4.y);
+                    const float2 g = ex2pos2(fma2(kc[p], rd, fma2(kl[p], rd, nd)));
+                    part[p] = fma2(g, SS ? fma2(nfi[p], wd, q) : q, part[p]);
+                }
+            }
+        }
+        if ((j + 2) % KCHUNK16 == 0 || j + 2 >= cnt2) {   // end of a run of KCHUNK16 sources
+#pragma unroll
+            for (int p = 0; p < 8; p++) {
+                kahan_add(sum[2 * p], cmp[2 * p], part[p].x);
+                kahan_add(sum[2 * p + 1], cmp[2 * p + 1], part[p].y);
+                part[p] = make_float2(0.f, 0.f);
+            }
+        }
+        rc = rn;
+        nc = nn;
+        wc = wn;
+    }
+}
+
+// Per-orbital constants of a 16-orbital item, as orbital pairs.
+__device__ __forceinline__ void group16_constants(const Fields &a, int g0, float2 (&kc)[8], float2 (&kl)[8],
+                                                  float *kmin) {
+    float km = 3.4e38f;
+#pragma unroll
+    for (int p = 0; p < 8; p++) {
+        float h0, l0, h1, l1;
+        const int o0 = g0 + 2 * p, o1 = o0 + 1;
+        split_f32(o0 < a.norb ? -a.kp64[o0] * LOG2E : 0.0, h0, l0);   // -k log2(e)
+        split_f32(o1 < a.norb ? -a.kp64[o1] * LOG2E : 0.0, h1, l1);
+        kc[p] = make_float2(h0, h1);
+        kl[p] = make_float2(l0, l1);
+        if (o0 < a.norb) km = fminf(km, a.kc32[o0]);
+        if (o1 < a.norb) km = fminf(km, a.kc32[o1]);
+    }
+    if (kmin) *kmin = km;
+}
+
+// Dynamic shared memory of near_group16: the source rows, then the charges.
+__host__ __device__ constexpr size_t near_group16_smem(int pass) {
+    return sizeof(float) * (size_t)GTILE * ((pass == 1 ? 7 : 4) + QS16);
+}
+
+template <bool SS, int PASS>
+__global__ void __launch_bounds__(FT, 2) near_group16(const __grid_constant__ Work w) {
+    constexpr int NR = PASS == 1 ? 7 : 4;
+    extern __shared__ __align__(16) float s_dyn[];
+    float(*s_src)[GTILE] = reinterpret_cast<float(*)[GTILE]>(s_dyn);
+    float *s_q = s_dyn + NR * GTILE;
+    __shared__ int s_item;
+    const int tid = threadIdx.x;
+    for (;;) {
+        const int item = next_item(w.queue, &s_item);
+        if (item >= w.nitems) break;
+        const int2 it = w.items[item];
+        const Fields &a = w.sys[it.y >> 16];
+        const int b = it.x, g0 = it.y & 0xffff;
+        const int bn = a.batch_node[b];
+        const int tb = a.tbegin[bn], te = a.tend[bn];
+        const double cbx = a.tcenter[3L * bn], cby = a.tcenter[3L * bn + 1], cbz = a.tcenter[3L * bn + 2];
+        float2 kc[8], kl[8];
+        float kmin;
+        group16_constants(a, g0, kc, kl, &kmin);
+        const int r0 = a.rng_off[b], r1 = a.rng_off[b + 1];
+        for (int base = tb; base < te; base += FT) {
+            const int i = base + tid;
+            const bool v = i < te;
+            const bool warp_busy = base + (tid & ~31) < te;
+            float2 tx, ty, tz, lx = dup2(0.f), ly = dup2(0.f), lz = dup2(0.f);
+            if (PASS == 1) {  // absolute hi/lo splits (see near_tile)
+                const float4 h = v ? a.thi[i] : make_float4(0.f, 0.f, 0.f, 0.f);
+                const float4 l = v ? a.tlo[i] : make_float4(0.f, 0.f, 0.f, 0.f);
+                tx = dup2(h.x);
+                ty = dup2(h.y);
+                tz = dup2(h.z);
+                lx = dup2(l.x);
+                ly = dup2(l.y);
+                lz = dup2(l.z);
+            } else {
+                tx = dup2(v ? (float)(a.tx[i] - cbx) : 0.f);
+                ty = dup2(v ? (float)(a.ty[i] - cby) : 0.f);
+                tz = dup2(v ? (float)(a.tz[i] - cbz) : 0.f);
+            }
+            float2 nfi[8];
+            float sum[16], cmp[16];
+#pragma unroll
+            for (int p = 0; p < 8; p++) {
+                const int o0 = g0 + 2 * p, o1 = o0 + 1;
+                nfi[p] = make_float2((v && o0 < a.norb) ? -a.ft32[(long)o0 * a.nt + i] : 0.f,
+                                     (v && o1 < a.norb) ? -a.ft32[(long)o1 * a.nt + i] : 0.f);
+            }
+#pragma unroll
+            for (int o = 0; o < 16; o++) {
+                sum[o] = 0.f;
+                cmp[o] = 0.f;
+            }
+            for (int e = r0; e < r1; e++) {
+                const int2 r = a.rng[e];
+                if (a.rng_dmin[e] * kmin > 127.f) continue;  // every orbital's term is exactly 0
+                const bool close = range_is_close(r);
+                if (close != (PASS == 1)) continue;
+                const int rb = range_begin(r);
+                for (int t0 = rb; t0 < r.y; t0 += GTILE) {
+                    const int cnt = min(GTILE, r.y - t0);
+                    const int cnt2 = (cnt + 1) & ~1;
+                    __syncthreads();
+                    for (int j = tid; j < cnt2; j += FT) {
+                        const bool real = j < cnt;
+                        const int jj = t0 + (real ? j : 0);   // padding: a copy of the first source
+                        if constexpr (PASS == 1) {
+                            const float4 h = a.shi[jj], l = a.slo[jj];
+                            s_src[0][j] = -h.x;
+                            s_src[1][j] = -h.y;
+                            s_src[2][j] = -h.z;
+                            s_src[4][j] = -l.x;
+                            s_src[5][j] = -l.y;
+                            s_src[6][j] = -l.z;
+                        } else {
+                            s_src[0][j] = -(float)(a.sx[jj] - cbx);
+                            s_src[1][j] = -(float)(a.sy[jj] - cby);
+                            s_src[2][j] = -(float)(a.sz[jj] - cbz);
+                        }
+                        s_src[3][j] = real ? a.w32[jj] : 0.f;
+                    }
+                    // a warp stages 8 sources x 4 orbitals: 32-byte global segments,
+                    // conflict-free shared writes with the QS16 stride
+                    for (int k = tid; k < ((cnt2 + 7) & ~7) * 16; k += FT) {
+                        const int jb = k >> 7, rem = k & 127;
+                        const int o = rem >> 3, j = (jb << 3) + (rem & 7);
+                        if (j >= cnt2) continue;
+                        const int orb = g0 + o;
+                        s_q[j * QS16 + o] = (j < cnt && orb < a.norb) ? a.q32[(long)orb * a.ns + t0 + j] : 0.f;
+                    }
+                    __syncthreads();
+                    if (!warp_busy) continue;
+                    if (PASS == 1)
+                        group16_tile<SS, true, true>(s_src, s_q, cnt2, tx, ty, tz, lx, ly, lz, nfi, kc, kl, sum, cmp);
+                    else
+                        group16_tile<SS, false, false>(s_src, s_q, cnt2, tx, ty, tz, lx, ly, lz, nfi, kc, kl, sum,
+                                                       cmp);
+                }
+            }
+            if (v) {
+#pragma unroll
+                for (int o = 0; o < 16; o++)
+                    if (g0 + o < a.norb) a.out[(long)(g0 + o) * a.nt + i] = (double)sum[o] - (double)cmp[o];
+            }
+        }
+    }
+}
+
+// One staged proxy grid against one target for 16 orbitals (see far_cluster
+// for the padded innermost axis; charges staged QS16 floats per proxy point).
+template <bool SS, int MAXN1, bool EXACT>
+__device__ __forceinline__ void far_group16_cluster(const float *__restrict__ s_q, const float *__restrict__ s_w,
+                                                    const float (*s_p)[MAXN1], int n1_in, float tx, float ty,
+                                                    float tz, const float2 (&nfi)[8], const float2 (&kc)[8],
+                                                    const float2 (&kl)[8], float (&sum)[16], float (&cmp)[16]) {
+    constexpr int MH = even_up<MAXN1>() / 2;
+    const int n1 = EXACT ? MAXN1 : n1_in;
+    const int n1p = n1 + (n1 & 1);
+    float2 dz2[MH];
+#pragma unroll
+    for (int m = 0; m < MH; m++) {
+        const float d0 = tz - s_p[2][2 * m < n1 ? 2 * m : 0];
+        const float d1 = tz - s_p[2][2 * m + 1 < n1 ? 2 * m + 1 : 0];
+        dz2[m] = make_float2(d0 * d0, d1 * d1);
+    }
+    int idx = 0;
+    for (int k1 = 0; k1 < n1; k1++) {
+        float2 part[8];
+#pragma unroll
+        for (int p = 0; p < 8; p++) part[p] = make_float2(0.f, 0.f);
+        const float dx = tx - s_p[0][k1];
+        const float dx2 = dx * dx;
+        for (int k2 = 0; k2 < n1; k2++) {
+            const float dy = ty - s_p[1][k2];
+            const float2 rxy = dup2(fmaf(dy, dy, dx2));
+#pragma unroll
+            for (int m = 0; m < MH; m++) {
+                if (2 * m < n1) {
+                    const float2 r2 = add2(rxy, dz2[m]);
+                    const float2 rr = mul2(r2, rsqrt2(r2));
+                    const float2 nl = nlog2r2(r2);
+                    const float2 wk = lds2(s_w + idx + 2 * m);
+#pragma unroll
+                    for (int u = 0; u < 2; u++) {
+                        const float2 rd = dup2(u ? rr.y : rr.x), nd = dup2(u ? nl.y : nl.x);
+                        const float2 wd = dup2(u ? wk.y : wk.x);
+                        const float *qk = s_q + (idx + 2 * m + u) * QS16;
+#pragma unroll
+                        for (int o4 = 0; o4 < 4; o4++) {
+                            const float4 q4 = lds4(qk + 4 * o4);
+#pragma unroll
+                            for (int h = 0; h < 2; h++) {
+                                const int p = 2 * o4 + h;
+                                const float2 q = h ? make_float2(q4.z, q4.w) : make_float2(q4.x, q4.y);
+                                const float2 g = ex2pos2(fma2(kc[p], rd, fma2(kl[p], rd, nd)));
+                                part[p] = fma2(g, SS ? fma2(nfi[p], wd, q) : q, part[p]);
+                            }
+                        }
+                    }
+                }
+            }
+            idx += n1p;
+        }
+#pragma unroll
+        for (int p = 0; p < 8; p++) {
+            kahan_add(sum[2 * p], cmp[2 * p], part[p].x);
+            kahan_add(sum[2 * p + 1], cmp[2 * p + 1], part[p].y);
+        }
+    }
+}
+
+// Dynamic shared memory of far_group16: charges (Pp * QS16 floats) then the
+// weight charges (Pp floats), Pp = n1 * n1 * n1p.
+__host__ __device__ constexpr size_t far_group16_smem(int n1) {
+    return sizeof(float) * (size_t)n1 * n1 * (n1 + (n1 & 1)) * (QS16 + 1);
+}
+
+template <bool SS, int MAXN1, bool EXACT>
+__global__ void __launch_bounds__(FT, 2) far_group16(const __grid_constant__ Work w) {
+    extern __shared__ __align__(16) float s_dyn[];
+    __shared__ float s_p[3][MAXN1];
+    __shared__ int s_item;
+    const int tid = threadIdx.x;
+    for (;;) {
+        const int item = next_item(w.queue, &s_item);
+        if (item >= w.nitems) break;
+        const int2 it = w.items[item];
+        const Fields &a = w.sys[it.y >> 16];
+        const int b = it.x, g0 = it.y & 0xffff;
+        const int n1 = EXACT ? MAXN1 : a.n1, P = EXACT ? MAXN1 * MAXN1 * MAXN1 : a.P;
+        const int n1p = n1 + (n1 & 1), Pp = n1 * n1 * n1p;
+        float *s_q = s_dyn;
+        float *s_w = s_dyn + (size_t)Pp * QS16;
+        const int f0 = a.far_off[b], f1 = a.far_off[b + 1];
+        if (f0 == f1) continue;
+        const int bn = a.batch_node[b];
+        const int tb = a.tbegin[bn], te = a.tend[bn];
+        const double cb[3] = {a.tcenter[3L * bn], a.tcenter[3L * bn + 1], a.tcenter[3L * bn + 2]};
+        float2 kc[8], kl[8];
+        group16_constants(a, g0, kc, kl, nullptr);
+        for (int base = tb; base < te; base += FT) {
+            const int i = base + tid;
+            const bool v = i < te;
+            const bool warp_busy = base + (tid & ~31) < te;
+            const float tx = v ? (float)(a.tx[i] - cb[0]) : 0.f;
+            const float ty = v ? (float)(a.ty[i] - cb[1]) : 0.f;
+            const float tz = v ? (float)(a.tz[i] - cb[2]) : 0.f;
+            float2 nfi[8];
+            float sum[16], cmp[16];
+#pragma unroll
+            for (int p = 0; p < 8; p++) {
+                const int o0 = g0 + 2 * p, o1 = o0 + 1;
+                nfi[p] = make_float2((v && o0 < a.norb) ? -a.ft32[(long)o0 * a.nt + i] : 0.f,
+                                     (v && o1 < a.norb) ? -a.ft32[(long)o1 * a.nt + i] : 0.f);
+            }
+#pragma unroll
+            for (int o = 0; o < 16; o++) {
+                sum[o] = 0.f;
+                cmp[o] = 0.f;
+            }
+            for (int e = f0; e < f1; e++) {
+                const int slot = a.node_slot[a.far_list[e]];
+                const double *gm = a.geom + 6L * slot;
+                __syncthreads();
+                // a warp stages 8 proxy points x 4 orbitals (see near_group16)
+                for (int k = tid; k < ((Pp + 7) & ~7) * 16; k += FT) {
+                    const int kb = k >> 7, rem = k & 127;
+                    const int o = rem >> 3, kk = (kb << 3) + (rem & 7);
+                    if (kk >= Pp) continue;
+                    const int row = kk / n1p, k3 = kk - row * n1p;
+                    const int orb = g0 + o;
+                    s_q[kk * QS16 + o] =
+                        (k3 < n1 && orb < a.norb) ? a.qhat32[((long)orb * a.nslots + slot) * P + row * n1 + k3] : 0.f;
+                }
+                for (int k = tid; k < Pp; k += FT) {
+                    const int row = k / n1p, k3 = k - row * n1p;
+                    s_w[k] = k3 < n1 ? a.what32[(long)slot * P + row * n1 + k3] : 0.f;
+                }
+                if (tid < 3 * n1) {
+                    const int d = tid / n1, m = tid - d * n1;
+                    const double cbd = d == 0 ? cb[0] : (d == 1 ? cb[1] : cb[2]);
+                    s_p[d][m] = (float)((gm[d] + gm[3 + d] * a.tn[m]) - cbd);
+                }
+                __syncthreads();
+                if (!warp_busy) continue;
+                far_group16_cluster<SS, MAXN1, EXACT>(s_q, s_w, s_p, n1, tx, ty, tz, nfi, kc, kl, sum, cmp);
+            }
+            if (v) {
+#pragma unroll
+                for (int o = 0; o < 16; o++)
+                    if (g0 + o < a.norb) a.out[(long)(g0 + o) * a.nt + i] = (double)sum[o] - (double)cmp[o];
+            }
+        }
+    }
+}
+
+// ---------------------------------------------------------------------------
 // FP64 near and far fields (the plain path).
 // ---------------------------------------------------------------------------
 template <int KERN, bool SS>
@@ -1120,12 +1484,12 @@ int occupancy_grid(K kern, int *grid, size_t smem = 0) {
 }
 
 // Persistent launch: grid = resident CTAs (at most one per work item).  smem
-// bytes of dynamic shared memory; above the 48 KB default the kernel's limit
-// is raised first.
+// bytes of dynamic shared memory; for large requests the kernel's limit is
+// raised first.
 template <typename K>
 int launch_persistent(K kern, const Work &w, cudaStream_t s, size_t smem = 0) {
     if (w.nitems == 0) return TAGI_OK;
-    if (smem > 48 * 1024)
+    if (smem > 32 * 1024)   // dynamic + static above the 48 KB default needs the opt-in
         TAGI_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
     int grid = 0;
     TAGI_TRY(occupancy_grid(kern, &grid, smem));
@@ -1261,27 +1625,104 @@ __global__ void __launch_bounds__(FT, 2) pair_peak_far_group(int reps, float *ou
     out[blockIdx.x * FT + threadIdx.x] = acc;
 }
 
+// The same two loops with 16 orbitals packed by orbital (near: 256-source
+// tiles, so the loop's operands fit static shared memory).
+constexpr int PEAK16_TILE = 256;
+template <bool SS>
+__global__ void __launch_bounds__(FT, 2) pair_peak_near_group16(int reps, float *out) {
+    __shared__ __align__(16) float s[4][GTILE];
+    __shared__ __align__(16) float s_q[PEAK16_TILE * QS16];
+    for (int j = threadIdx.x; j < PEAK16_TILE; j += FT) {
+        const float v = (float)((j * 37) % 101) * 0.01f - 0.5f;
+        s[0][j] = -v;
+        s[1][j] = -(0.3f * v + 0.1f);
+        s[2][j] = -(0.7f - v);
+        s[3][j] = 0.25f;
+    }
+    for (int k = threadIdx.x; k < PEAK16_TILE * QS16; k += FT) s_q[k] = 0.5f + 0.001f * k;
+    __syncthreads();
+    const float2 tx = dup2(0.01f * (threadIdx.x & 31)), ty = dup2(0.02f), tz = dup2(-0.03f * (threadIdx.x >> 5));
+    float2 nfi[8], kc[8], kl[8];
+    float sum[16], cmp[16];
+#pragma unroll
+    for (int p = 0; p < 8; p++) {
+        float h0, l0, h1, l1;
+        split_f32(-(0.5 + 0.3 * (2 * p)) * LOG2E, h0, l0);
+        split_f32(-(0.5 + 0.3 * (2 * p + 1)) * LOG2E, h1, l1);
+        kc[p] = make_float2(h0, h1);
+        kl[p] = make_float2(l0, l1);
+        nfi[p] = dup2(-0.3f);
+    }
+#pragma unroll
+    for (int o = 0; o < 16; o++) sum[o] = cmp[o] = 0.f;
+    const float2 z = dup2(0.f);
+    for (int r = 0; r < reps; r++)
+        group16_tile<SS, false, false>(s, s_q, PEAK16_TILE, tx, ty, tz, z, z, z, nfi, kc, kl, sum, cmp);
+    float acc = 0.f;
+#pragma unroll
+    for (int o = 0; o < 16; o++) acc += sum[o] - cmp[o];
+    out[blockIdx.x * FT + threadIdx.x] = acc;
+}
+
+template <bool SS>
+__global__ void __launch_bounds__(FT, 2) pair_peak_far_group16(int reps, float *out) {
+    constexpr int N1 = 8, PP = N1 * N1 * N1;
+    __shared__ __align__(16) float s_q[PP * QS16];
+    __shared__ __align__(16) float s_w[PP];
+    __shared__ float s_p[3][N1];
+    for (int k = threadIdx.x; k < PP * QS16; k += FT) s_q[k] = 0.5f + 0.001f * k;
+    for (int k = threadIdx.x; k < PP; k += FT) s_w[k] = 0.25f;
+    if (threadIdx.x < 3 * N1) s_p[threadIdx.x / N1][threadIdx.x % N1] = 1.0f + 0.1f * threadIdx.x;
+    __syncthreads();
+    const float tx = 0.01f * (threadIdx.x & 31), ty = 0.02f, tz = -0.03f * (threadIdx.x >> 5);
+    float2 nfi[8], kc[8], kl[8];
+    float sum[16], cmp[16];
+#pragma unroll
+    for (int p = 0; p < 8; p++) {
+        float h0, l0, h1, l1;
+        split_f32(-(0.5 + 0.3 * (2 * p)) * LOG2E, h0, l0);
+        split_f32(-(0.5 + 0.3 * (2 * p + 1)) * LOG2E, h1, l1);
+        kc[p] = make_float2(h0, h1);
+        kl[p] = make_float2(l0, l1);
+        nfi[p] = dup2(-0.3f);
+    }
+#pragma unroll
+    for (int o = 0; o < 16; o++) sum[o] = cmp[o] = 0.f;
+    for (int r = 0; r < reps; r++)
+        far_group16_cluster<SS, N1, true>(s_q, s_w, s_p, N1, tx, ty, tz, nfi, kc, kl, sum, cmp);
+    float acc = 0.f;
+#pragma unroll
+    for (int o = 0; o < 16; o++) acc += sum[o] - cmp[o];
+    out[blockIdx.x * FT + threadIdx.x] = acc;
+}
+
 template <int KERN, bool SS>
 int launch_pair_peak(int variant, int grid, int reps, float *out, cudaStream_t s) {
     if (variant == 0) launch(pair_peak_near<KERN, SS>, grid, FT, 0, s, reps, out);
     else if (variant == 1) launch(pair_peak_far<KERN, SS>, grid, FT, 0, s, reps, out);
     else if (variant == 2) launch(pair_peak_near_group<SS>, grid, FT, 0, s, reps, out);
-    else launch(pair_peak_far_group<SS>, grid, FT, 0, s, reps, out);
+    else if (variant == 3) launch(pair_peak_far_group<SS>, grid, FT, 0, s, reps, out);
+    else if (variant == 4) launch(pair_peak_near_group16<SS>, grid, FT, 0, s, reps, out);
+    else launch(pair_peak_far_group16<SS>, grid, FT, 0, s, reps, out);
     TAGI_LAUNCH_CHECK();
     return TAGI_OK;
 }
 
 template <int KERN, bool SS>
 int run_pair_peak(int variant, double *pairs_per_s, cudaStream_t s) {
-    if (variant < 0 || variant > 3)
-        return set_error(TAGI_ERR_ARG, "pair peak variant %d (0 near, 1 far, 2 near group, 3 far group)", variant);
+    if (variant < 0 || variant > 5)
+        return set_error(TAGI_ERR_ARG,
+                         "pair peak variant %d (0 near, 1 far, 2 near group, 3 far group, 4 near group of 16, "
+                         "5 far group of 16)", variant);
     if (variant >= 2 && KERN != KERNEL_YUKAWA)
         return set_error(TAGI_ERR_UNSUPPORTED, "orbital-group kernels are Yukawa only");
     int grid = 0;
     if (variant == 0) TAGI_TRY(occupancy_grid(pair_peak_near<KERN, SS>, &grid));
     else if (variant == 1) TAGI_TRY(occupancy_grid(pair_peak_far<KERN, SS>, &grid));
     else if (variant == 2) TAGI_TRY(occupancy_grid(pair_peak_near_group<SS>, &grid));
-    else TAGI_TRY(occupancy_grid(pair_peak_far_group<SS>, &grid));
+    else if (variant == 3) TAGI_TRY(occupancy_grid(pair_peak_far_group<SS>, &grid));
+    else if (variant == 4) TAGI_TRY(occupancy_grid(pair_peak_near_group16<SS>, &grid));
+    else TAGI_TRY(occupancy_grid(pair_peak_far_group16<SS>, &grid));
     Arena tmp;
     tmp.stream = s;
     float *out = nullptr;
@@ -1289,8 +1730,9 @@ int run_pair_peak(int variant, double *pairs_per_s, cudaStream_t s) {
     cudaEvent_t a, b;
     cudaEventCreate(&a);
     cudaEventCreate(&b);
-    // pairs per repetition per thread: two targets x a tile, or one target x a tile x 8 orbitals
-    const int per_rep = variant == 0 ? 2 * NTILE : (variant == 1 ? 2 * 512 : (variant == 2 ? GTILE * 8 : 512 * 8));
+    // pairs per repetition per thread: two targets x a tile, or one target x a tile x 8 (16) orbitals
+    const int per_rep_of[6] = {2 * NTILE, 2 * 512, GTILE * 8, 512 * 8, PEAK16_TILE * 16, 512 * 16};
+    const int per_rep = per_rep_of[variant];
     int reps = 16;
     float ms = 0.f;
     int rc = TAGI_OK;
@@ -1342,6 +1784,24 @@ int launch_fields(const SysCall *calls, const Fields *f, int nsys, const Schedul
     wf.queue = queue + 1;
     const bool one = sh.nt == 1;
     phase_mark(PH_NEAR, true, s);
+    if (precision == PREC_MIXED && KERN == KERNEL_YUKAWA && sh.og == 16) {
+        TAGI_TRY(launch_persistent(near_group16<SS, 0>, wn, s, near_group16_smem(0)));
+        phase_mark(PH_NEAR, false, s);
+        phase_mark(PH_NEAR_CLOSE, true, s);
+        TAGI_TRY(launch_persistent(near_group16<SS, 1>, wc, s, near_group16_smem(1)));
+        phase_mark(PH_NEAR_CLOSE, false, s);
+        phase_mark(PH_FAR, true, s);
+        if (sh.maxn1 <= 4)
+            TAGI_TRY(launch_persistent(far_group16<SS, 4, false>, wf, s, far_group16_smem(sh.maxn1)));
+        else if (sh.maxn1 == 8 && sh.minn1 == 8)   // degree 7 everywhere: fixed loops
+            TAGI_TRY(launch_persistent(far_group16<SS, 8, true>, wf, s, far_group16_smem(8)));
+        else if (sh.maxn1 <= 8)
+            TAGI_TRY(launch_persistent(far_group16<SS, 8, false>, wf, s, far_group16_smem(sh.maxn1)));
+        else
+            TAGI_TRY(launch_persistent(far_group16<SS, MAX_DEGREE + 1, false>, wf, s, far_group16_smem(sh.maxn1)));
+        phase_mark(PH_FAR, false, s);
+        return TAGI_OK;
+    }
     if (precision == PREC_MIXED && KERN == KERNEL_YUKAWA && sh.og > 1) {
         // orbital groups share the geometry of each pair across og orbitals
         const bool g8 = sh.og == 8;
@@ -1525,12 +1985,18 @@ int ensure_scratch(Plan &p, int norb) {
 }
 
 // Orbitals per work item: Yukawa in mixed precision shares each pair's
-// geometry across a group of 8 (or 4) orbitals once the largest system has
-// that many; everything else runs one orbital per item.  requested > 0
-// (1, 4 or 8) overrides the choice where the kernel supports it.
-int orbitals_per_item(int kernel, int precision, int max_norb, int requested) {
+// geometry across a group of 16, 8 or 4 orbitals once the largest system has
+// that many; everything else runs one orbital per item.  16 is taken up to
+// degree 7 (above it a 16-orbital proxy grid no longer fits two CTAs per SM)
+// when its padded orbital slots, at GROUP16_COST of a group-of-8 slot's time,
+// cost less than the group-of-8 slots.  requested > 0 (1, 4, 8 or 16)
+// overrides the choice where the kernel supports it.
+constexpr double GROUP16_COST = 0.85;
+int orbitals_per_item(int kernel, int precision, int max_norb, int requested, int max_n1) {
     if (kernel != KERNEL_YUKAWA || precision != PREC_MIXED) return 1;
-    if (requested == 1 || requested == 4 || requested == 8) return requested;
+    if (requested == 1 || requested == 4 || requested == 8 || requested == 16) return requested;
+    const double slots16 = 16.0 * ((max_norb + 15) / 16), slots8 = 8.0 * ((max_norb + 7) / 8);
+    if (max_norb >= 16 && max_n1 <= 8 && GROUP16_COST * slots16 < slots8) return 16;
     return max_norb >= 8 ? 8 : (max_norb >= 4 ? 4 : 1);
 }
 
@@ -1682,7 +2148,7 @@ int convolve_systems(SysCall *calls, int nsys, int kernel, int singularity, int 
 int convolve(Plan &p, const double *tv, const double *sv, double *out, int norb, int kernel,
              const double *kparams, int nkp, int singularity, int precision, cudaStream_t s, bool kp_device,
              int og_request, int nt_request) {
-    const int og = orbitals_per_item(kernel, precision, norb, og_request);
+    const int og = orbitals_per_item(kernel, precision, norb, og_request, p.n1);
     const Schedule *sc = nullptr;
     for (const Schedule &c : p.scheds)
         if (schedule_matches(c, &norb, 1, og)) sc = &c;

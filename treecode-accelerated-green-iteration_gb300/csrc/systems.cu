@@ -62,8 +62,9 @@ int tagi_plan_convolve_ex(tagi_plan *plan, int numOrbitals, const double *target
     if (numOrbitals < 1 || numOrbitals > 0xffff)
         return set_error(TAGI_ERR_ARG, "numOrbitals %d outside [1, 65535]", numOrbitals);
     if (!targetValues || !sourceValues || !output) return set_error(TAGI_ERR_ARG, "null device pointer");
-    if (orbitalsPerItem != 0 && orbitalsPerItem != 1 && orbitalsPerItem != 4 && orbitalsPerItem != 8)
-        return set_error(TAGI_ERR_ARG, "orbitalsPerItem %d must be 0 (automatic), 1, 4 or 8", orbitalsPerItem);
+    if (orbitalsPerItem != 0 && orbitalsPerItem != 1 && orbitalsPerItem != 4 && orbitalsPerItem != 8 &&
+        orbitalsPerItem != 16)
+        return set_error(TAGI_ERR_ARG, "orbitalsPerItem %d must be 0 (automatic), 1, 4, 8 or 16", orbitalsPerItem);
     if (targetsPerThread < 0 || targetsPerThread > 2)
         return set_error(TAGI_ERR_ARG, "targetsPerThread %d must be 0 (automatic), 1 or 2", targetsPerThread);
     TAGI_TRY(check_call(kernel, singularity, precision));
@@ -95,8 +96,9 @@ int tagi_systems_create(tagi_systems **systems, int numSystems, tagi_plan *const
     if (numSystems < 1 || numSystems > MAX_SYSTEMS)
         return set_error(TAGI_ERR_ARG, "numSystems %d outside [1, %d]", numSystems, MAX_SYSTEMS);
     if (!plans || !numOrbitals) return set_error(TAGI_ERR_ARG, "null plans or numOrbitals");
-    if (orbitalsPerItem != 0 && orbitalsPerItem != 1 && orbitalsPerItem != 4 && orbitalsPerItem != 8)
-        return set_error(TAGI_ERR_ARG, "orbitalsPerItem %d must be 0 (automatic), 1, 4 or 8", orbitalsPerItem);
+    if (orbitalsPerItem != 0 && orbitalsPerItem != 1 && orbitalsPerItem != 4 && orbitalsPerItem != 8 &&
+        orbitalsPerItem != 16)
+        return set_error(TAGI_ERR_ARG, "orbitalsPerItem %d must be 0 (automatic), 1, 4, 8 or 16", orbitalsPerItem);
     if (targetsPerThread < 0 || targetsPerThread > 2)
         return set_error(TAGI_ERR_ARG, "targetsPerThread %d must be 0 (automatic), 1 or 2", targetsPerThread);
     TAGI_TRY(check_call(kernel, SING_SUBTRACTION, precision));
@@ -116,7 +118,9 @@ int tagi_systems_create(tagi_systems **systems, int numSystems, tagi_plan *const
         y->plans.push_back(reinterpret_cast<Plan *>(plans[i]));
         y->norb.push_back(numOrbitals[i]);
     }
-    const int og = orbitals_per_item(kernel, precision, maxo, orbitalsPerItem);
+    int maxn1 = 0;
+    for (Plan *q : y->plans) maxn1 = q->n1 > maxn1 ? q->n1 : maxn1;
+    const int og = orbitals_per_item(kernel, precision, maxo, orbitalsPerItem, maxn1);
     int rc = build_schedule(y->plans.data(), y->norb.data(), numSystems, og, y->sched, y->stream);
     if (!rc) {
         void *v = nullptr;
