@@ -951,11 +951,18 @@ __global__ void __launch_bounds__(FT, 2) far_group_db(const __grid_constant__ Wo
 constexpr int QS16 = 20;
 constexpr int KCHUNK16 = 32;
 
+// One tile of cnt4 sources (a multiple of 4) for 16 orbitals.  Four sources
+// per iteration (two packed pairs), software pipelined: the next four
+// sources' geometry (loads, rsqrt, lg2) is issued before this iteration's
+// 64 orbital-pair updates, which hides its latency.  The per-orbital Kahan
+// sums live in shared memory (s_k[o][FT] sums, s_k[16 + o][FT]
+// compensations, touched once per KCHUNK16 sources), which leaves the
+// registers for the pipelined geometry.
 template <bool SS, bool MASK, bool PRECISE>
 __device__ __forceinline__ void group16_tile(const float (*__restrict__ s)[GTILE], const float *__restrict__ s_q,
-                                             int cnt2, float2 tx, float2 ty, float2 tz, float2 lx, float2 ly,
+                                             int cnt4, float2 tx, float2 ty, float2 tz, float2 lx, float2 ly,
                                              float2 lz, const float2 (&nfi)[8], const float2 (&kc)[8],
-                                             const float2 (&kl)[8], float (&sum)[16], float (&cmp)[16]) {
+                                             const float2 (&kl)[8], float *__restrict__ s_k) {
     // r, -log2 r and w of the source pair at j (packed over the two sources)
     auto geometry = [&](int j, float2 &r, float2 &nl, float2 &wv) {
         float2 dx = add2(tx, lds2(s[0] + j)), dy = add2(ty, lds2(s[1] + j)), dz = add2(tz, lds2(s[2] + j));
@@ -976,20 +983,25 @@ __device__ __forceinline__ void group16_tile(const float (*__restrict__ s)[GTILE
         }
         r = mul2(r2, rinv);
     };
+    const int tid = threadIdx.x;
     float2 part[8];
 #pragma unroll
     for (int p = 0; p < 8; p++) part[p] = make_float2(0.f, 0.f);
-    // software pipelined: the next pair's geometry (loads, rsqrt, lg2) is
-    // issued before this pair's 16-orbital work, which hides its latency
-    float2 rc, nc, wc;
-    geometry(0, rc, nc, wc);
+    float2 rc[2], nc[2], wc[2];
+    geometry(0, rc[0], nc[0], wc[0]);
+    geometry(2, rc[1], nc[1], wc[1]);
 #pragma unroll 1
-    for (int j = 0; j < cnt2; j += 2) {
-        float2 rn, nn, wn;
-        geometry(j + 2 < cnt2 ? j + 2 : j, rn, nn, wn);
+    for (int j = 0; j < cnt4; j += 4) {
+        const int jn = j + 4 < cnt4 ? j + 4 : j;
+        float2 rn[2], nn[2], wn[2];
+        geometry(jn, rn[0], nn[0], wn[0]);
+        geometry(jn + 2, rn[1], nn[1], wn[1]);
 #pragma unroll
-        for (int u = 0; u < 2; u++) {
-            const float2 rd = dup2(u ? rc.y : rc.x), nd = dup2(u ? nc.y : nc.x), wd = dup2(u ? wc.y : wc.x);
+        for (int u = 0; u < 4; u++) {
+            const float ru = (u & 1) ? rc[u >> 1].y : rc[u >> 1].x;
+            const float nu = (u & 1) ? nc[u >> 1].y : nc[u >> 1].x;
+            const float wu = (u & 1) ? wc[u >> 1].y : wc[u >> 1].x;
+            const float2 rd = dup2(ru), nd = dup2(nu), wd = dup2(wu);
             const float *qj = s_q + (j + u) * QS16;
 #pragma unroll
             for (int o4 = 0; o4 < 4; o4++) {
@@ -1003,17 +1015,26 @@ __device__ __forceinline__ void group16_tile(const float (*__restrict__ s)[GTILE
                 }
             }
         }
-        if ((j + 2) % KCHUNK16 == 0 || j + 2 >= cnt2) {   // end of a run of KCHUNK16 sources
+        if ((j + 4) % KCHUNK16 == 0 || j + 4 >= cnt4) {   // end of a run of KCHUNK16 sources
 #pragma unroll
             for (int p = 0; p < 8; p++) {
-                kahan_add(sum[2 * p], cmp[2 * p], part[p].x);
-                kahan_add(sum[2 * p + 1], cmp[2 * p + 1], part[p].y);
+#pragma unroll
+                for (int h = 0; h < 2; h++) {
+                    const int o = 2 * p + h;
+                    float sm = s_k[o * FT + tid], cm = s_k[(16 + o) * FT + tid];
+                    kahan_add(sm, cm, h ? part[p].y : part[p].x);
+                    s_k[o * FT + tid] = sm;
+                    s_k[(16 + o) * FT + tid] = cm;
+                }
                 part[p] = make_float2(0.f, 0.f);
             }
         }
-        rc = rn;
-        nc = nn;
-        wc = wn;
+#pragma unroll
+        for (int v = 0; v < 2; v++) {
+            rc[v] = rn[v];
+            nc[v] = nn[v];
+            wc[v] = wn[v];
+        }
     }
 }
 
@@ -1035,9 +1056,10 @@ __device__ __forceinline__ void group16_constants(const Fields &a, int g0, float
     if (kmin) *kmin = km;
 }
 
-// Dynamic shared memory of near_group16: the source rows, then the charges.
+// Dynamic shared memory of near_group16: the source rows, the charges, then
+// the per-thread Kahan sums and compensations of 16 orbitals.
 __host__ __device__ constexpr size_t near_group16_smem(int pass) {
-    return sizeof(float) * (size_t)GTILE * ((pass == 1 ? 7 : 4) + QS16);
+    return sizeof(float) * ((size_t)GTILE * ((pass == 1 ? 7 : 4) + QS16) + 32 * FT);
 }
 
 template <bool SS, int PASS>
@@ -1046,6 +1068,7 @@ __global__ void __launch_bounds__(FT, 2) near_group16(const __grid_constant__ Wo
     extern __shared__ __align__(16) float s_dyn[];
     float(*s_src)[GTILE] = reinterpret_cast<float(*)[GTILE]>(s_dyn);
     float *s_q = s_dyn + NR * GTILE;
+    float *s_k = s_q + GTILE * QS16;
     __shared__ int s_item;
     const int tid = threadIdx.x;
     for (;;) {
@@ -1081,7 +1104,6 @@ __global__ void __launch_bounds__(FT, 2) near_group16(const __grid_constant__ Wo
                 tz = dup2(v ? (float)(a.tz[i] - cbz) : 0.f);
             }
             float2 nfi[8];
-            float sum[16], cmp[16];
 #pragma unroll
             for (int p = 0; p < 8; p++) {
                 const int o0 = g0 + 2 * p, o1 = o0 + 1;
@@ -1089,10 +1111,7 @@ __global__ void __launch_bounds__(FT, 2) near_group16(const __grid_constant__ Wo
                                      (v && o1 < a.norb) ? -a.ft32[(long)o1 * a.nt + i] : 0.f);
             }
 #pragma unroll
-            for (int o = 0; o < 16; o++) {
-                sum[o] = 0.f;
-                cmp[o] = 0.f;
-            }
+            for (int o = 0; o < 32; o++) s_k[o * FT + tid] = 0.f;   // this thread's own sums
             for (int e = r0; e < r1; e++) {
                 const int2 r = a.rng[e];
                 if (a.rng_dmin[e] * kmin > 127.f) continue;  // every orbital's term is exactly 0
@@ -1101,9 +1120,9 @@ __global__ void __launch_bounds__(FT, 2) near_group16(const __grid_constant__ Wo
                 const int rb = range_begin(r);
                 for (int t0 = rb; t0 < r.y; t0 += GTILE) {
                     const int cnt = min(GTILE, r.y - t0);
-                    const int cnt2 = (cnt + 1) & ~1;
+                    const int cnt4 = (cnt + 3) & ~3;
                     __syncthreads();
-                    for (int j = tid; j < cnt2; j += FT) {
+                    for (int j = tid; j < cnt4; j += FT) {
                         const bool real = j < cnt;
                         const int jj = t0 + (real ? j : 0);   // padding: a copy of the first source
                         if constexpr (PASS == 1) {
@@ -1123,26 +1142,26 @@ __global__ void __launch_bounds__(FT, 2) near_group16(const __grid_constant__ Wo
                     }
                     // a warp stages 8 sources x 4 orbitals: 32-byte global segments,
                     // conflict-free shared writes with the QS16 stride
-                    for (int k = tid; k < ((cnt2 + 7) & ~7) * 16; k += FT) {
+                    for (int k = tid; k < ((cnt4 + 7) & ~7) * 16; k += FT) {
                         const int jb = k >> 7, rem = k & 127;
                         const int o = rem >> 3, j = (jb << 3) + (rem & 7);
-                        if (j >= cnt2) continue;
+                        if (j >= cnt4) continue;
                         const int orb = g0 + o;
                         s_q[j * QS16 + o] = (j < cnt && orb < a.norb) ? a.q32[(long)orb * a.ns + t0 + j] : 0.f;
                     }
                     __syncthreads();
                     if (!warp_busy) continue;
                     if (PASS == 1)
-                        group16_tile<SS, true, true>(s_src, s_q, cnt2, tx, ty, tz, lx, ly, lz, nfi, kc, kl, sum, cmp);
+                        group16_tile<SS, true, true>(s_src, s_q, cnt4, tx, ty, tz, lx, ly, lz, nfi, kc, kl, s_k);
                     else
-                        group16_tile<SS, false, false>(s_src, s_q, cnt2, tx, ty, tz, lx, ly, lz, nfi, kc, kl, sum,
-                                                       cmp);
+                        group16_tile<SS, false, false>(s_src, s_q, cnt4, tx, ty, tz, lx, ly, lz, nfi, kc, kl, s_k);
                 }
             }
             if (v) {
 #pragma unroll
                 for (int o = 0; o < 16; o++)
-                    if (g0 + o < a.norb) a.out[(long)(g0 + o) * a.nt + i] = (double)sum[o] - (double)cmp[o];
+                    if (g0 + o < a.norb)
+                        a.out[(long)(g0 + o) * a.nt + i] = (double)s_k[o * FT + tid] - (double)s_k[(16 + o) * FT + tid];
             }
         }
     }
@@ -1625,13 +1644,15 @@ __global__ void __launch_bounds__(FT, 2) pair_peak_far_group(int reps, float *ou
     out[blockIdx.x * FT + threadIdx.x] = acc;
 }
 
-// The same two loops with 16 orbitals packed by orbital (near: 256-source
-// tiles, so the loop's operands fit static shared memory).
-constexpr int PEAK16_TILE = 256;
+// The same two loops with 16 orbitals packed by orbital (near: shared memory
+// laid out as near_group16's, dynamic).
+constexpr int PEAK16_TILE = GTILE;
 template <bool SS>
 __global__ void __launch_bounds__(FT, 2) pair_peak_near_group16(int reps, float *out) {
-    __shared__ __align__(16) float s[4][GTILE];
-    __shared__ __align__(16) float s_q[PEAK16_TILE * QS16];
+    extern __shared__ __align__(16) float s_dyn[];
+    float(*s)[GTILE] = reinterpret_cast<float(*)[GTILE]>(s_dyn);
+    float *s_q = s_dyn + 4 * GTILE;
+    float *s_k = s_q + GTILE * QS16;
     for (int j = threadIdx.x; j < PEAK16_TILE; j += FT) {
         const float v = (float)((j * 37) % 101) * 0.01f - 0.5f;
         s[0][j] = -v;
@@ -1643,7 +1664,6 @@ __global__ void __launch_bounds__(FT, 2) pair_peak_near_group16(int reps, float 
     __syncthreads();
     const float2 tx = dup2(0.01f * (threadIdx.x & 31)), ty = dup2(0.02f), tz = dup2(-0.03f * (threadIdx.x >> 5));
     float2 nfi[8], kc[8], kl[8];
-    float sum[16], cmp[16];
 #pragma unroll
     for (int p = 0; p < 8; p++) {
         float h0, l0, h1, l1;
@@ -1653,14 +1673,12 @@ __global__ void __launch_bounds__(FT, 2) pair_peak_near_group16(int reps, float 
         kl[p] = make_float2(l0, l1);
         nfi[p] = dup2(-0.3f);
     }
-#pragma unroll
-    for (int o = 0; o < 16; o++) sum[o] = cmp[o] = 0.f;
+    for (int o = 0; o < 32; o++) s_k[o * FT + threadIdx.x] = 0.f;
     const float2 z = dup2(0.f);
     for (int r = 0; r < reps; r++)
-        group16_tile<SS, false, false>(s, s_q, PEAK16_TILE, tx, ty, tz, z, z, z, nfi, kc, kl, sum, cmp);
+        group16_tile<SS, false, false>(s, s_q, PEAK16_TILE, tx, ty, tz, z, z, z, nfi, kc, kl, s_k);
     float acc = 0.f;
-#pragma unroll
-    for (int o = 0; o < 16; o++) acc += sum[o] - cmp[o];
+    for (int o = 0; o < 16; o++) acc += s_k[o * FT + threadIdx.x] - s_k[(16 + o) * FT + threadIdx.x];
     out[blockIdx.x * FT + threadIdx.x] = acc;
 }
 
@@ -1702,7 +1720,7 @@ int launch_pair_peak(int variant, int grid, int reps, float *out, cudaStream_t s
     else if (variant == 1) launch(pair_peak_far<KERN, SS>, grid, FT, 0, s, reps, out);
     else if (variant == 2) launch(pair_peak_near_group<SS>, grid, FT, 0, s, reps, out);
     else if (variant == 3) launch(pair_peak_far_group<SS>, grid, FT, 0, s, reps, out);
-    else if (variant == 4) launch(pair_peak_near_group16<SS>, grid, FT, 0, s, reps, out);
+    else if (variant == 4) launch(pair_peak_near_group16<SS>, grid, FT, near_group16_smem(0), s, reps, out);
     else launch(pair_peak_far_group16<SS>, grid, FT, 0, s, reps, out);
     TAGI_LAUNCH_CHECK();
     return TAGI_OK;
@@ -1721,7 +1739,11 @@ int run_pair_peak(int variant, double *pairs_per_s, cudaStream_t s) {
     else if (variant == 1) TAGI_TRY(occupancy_grid(pair_peak_far<KERN, SS>, &grid));
     else if (variant == 2) TAGI_TRY(occupancy_grid(pair_peak_near_group<SS>, &grid));
     else if (variant == 3) TAGI_TRY(occupancy_grid(pair_peak_far_group<SS>, &grid));
-    else if (variant == 4) TAGI_TRY(occupancy_grid(pair_peak_near_group16<SS>, &grid));
+    else if (variant == 4) {
+        TAGI_CUDA(cudaFuncSetAttribute(pair_peak_near_group16<SS>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                       (int)near_group16_smem(0)));
+        TAGI_TRY(occupancy_grid(pair_peak_near_group16<SS>, &grid, near_group16_smem(0)));
+    }
     else TAGI_TRY(occupancy_grid(pair_peak_far_group16<SS>, &grid));
     Arena tmp;
     tmp.stream = s;
