@@ -192,8 +192,8 @@ def tune_systems(meshes, values, kernel_params, kernel, singularity, precision="
                                             source_leaf=r["source_leaf"], target_leaf=r["target_leaf"],
                                             stream=stream)
              for (x, y, z, w), r in zip(meshes, per)]
-    # the joint launch is timed on up to 8 orbitals per system, so every group size can be tried
-    ns = [max(1, min(v.reshape(v.shape[0], -1).shape[0], max(sample_orbitals, 8))) for v in values]
+    # the joint launch is timed on up to 16 orbitals per system, so every group size can be tried
+    ns = [max(1, min(v.reshape(v.shape[0], -1).shape[0], max(sample_orbitals, 16))) for v in values]
     vs = [v.reshape(v.shape[0], -1)[:m].contiguous() for v, m in zip(values, ns)]
     ks = [np.asarray(k, dtype=np.float64).reshape(-1)[:m] for k, m in zip(kernel_params, ns)]
     outs = [torch.empty_like(v) for v in vs]

@@ -2013,7 +2013,7 @@ int ensure_scratch(Plan &p, int norb) {
 // when its padded orbital slots, at GROUP16_COST of a group-of-8 slot's time,
 // cost less than the group-of-8 slots.  requested > 0 (1, 4, 8 or 16)
 // overrides the choice where the kernel supports it.
-constexpr double GROUP16_COST = 0.85;
+constexpr double GROUP16_COST = 0.86;
 int orbitals_per_item(int kernel, int precision, int max_norb, int requested, int max_n1) {
     if (kernel != KERNEL_YUKAWA || precision != PREC_MIXED) return 1;
     if (requested == 1 || requested == 4 || requested == 8 || requested == 16) return requested;
