@@ -1602,12 +1602,16 @@ def twomesh_arm(args):
     k_ms = prof_ms[3] if dominant == "near" else prof_ms[4]
     # the phase holds two launches per step: the Hartree convolution (one
     # orbital, near_mixed/far_mixed) and the 21 Yukawa orbitals (orbital
-    # groups of 8): its pipe-bound time is the sum of both launches' ops
+    # groups as the library chooses them): its pipe-bound time is the sum of
+    # both launches' ops (per orbital convolution; padded group slots not counted)
     rates = pipe_rates(L, nat, torch.cuda.current_stream())
     n1 = DEGREE + 3
+    og_c = ctypes.c_int()
+    nat.check(L.tagi_orbitals_per_item(int(pkg.BaryTreeInterface.Kernel.YUKAWA), nat.PREC_MIXED, 21, 0, n1 - 1,
+                                       ctypes.byref(og_c)))
     pairs1 = (near_pairs if dominant == "near" else far_pairs) / 22.0
     mixes = ((pairs1, field_ops(f"{dominant}_mixed", "coulomb_ss", 1, n1)),
-             (21 * pairs1, field_ops(f"{dominant}_group", "yukawa_ss", 8, n1)))
+             (21 * pairs1, field_ops(f"{dominant}_group", "yukawa_ss", og_c.value, n1)))
     fp32 = max(rates["ffma"], rates["ffma2"])
     t_fma = sum(u * o[0] for u, o in mixes) / fp32
     t_mufu = sum(u * mufu_seconds(o, rates) for u, o in mixes)
@@ -1632,7 +1636,7 @@ def twomesh_arm(args):
                                   enumerate(("tree", "lists", "upward", "near", "far", "glue", "near_close"))},
             "roofline": {"bound": "fp32" if t_fma >= t_mufu else "mufu",
                          "kernel": f"{dominant} field: {dominant}_mixed (Hartree) + {dominant}_group (21 Yukawa "
-                                   "orbitals, groups of 8)",
+                                   f"orbitals, groups of {og_c.value})",
                          "achieved": achieved / 1e9, "peak": achieved / 1e9 * k_ms / bound_ms,
                          "unit": "Gpair-orbitals/s", "frac": bound_ms / k_ms, "traffic": None,
                          "pipe_frac": {"fp32": t_fma * 1e3 / k_ms, "mufu": t_mufu * 1e3 / k_ms},

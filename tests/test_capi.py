@@ -59,7 +59,7 @@ def test_host_only_entry_points(native):
 
 
 def test_orbital_group_choice(native):
-    """Automatic orbitals per item: 16 when its padded slots cost less than 8's, up to degree 7."""
+    """Automatic orbitals per item by the measured group cost model, groups of 16 up to degree 7."""
     L = native.lib()
     og = ctypes.c_int()
 
@@ -68,8 +68,9 @@ def test_orbital_group_choice(native):
         return og.value
 
     assert choose(32) == 16 and choose(16) == 16 and choose(28) == 16
-    assert choose(21) == 8 and choose(17) == 8 and choose(24) == 8   # 16-slots padding costs more
-    assert choose(32, degree=9) == 8 and choose(5) == 4 and choose(3) == 1
+    assert choose(21) == 16 and choose(17) == 16 and choose(24) == 16 and choose(9) == 16
+    assert choose(8) == 8 and choose(7) == 8 and choose(6) == 16 and choose(5) == 16 and choose(4) == 4
+    assert choose(32, degree=9) == 8 and choose(5, degree=9) == 8 and choose(3) == 1
     assert choose(32, requested=8) == 8 and choose(3, requested=16) == 16
     assert choose(32, precision=native.PREC_FP64) == 1 and choose(32, kernel=1) == 1
     assert L.tagi_orbitals_per_item(2, 0, 32, 12, 7, ctypes.byref(og)) == native.TAGI_ERR_ARG

@@ -38,7 +38,7 @@ def test_systems_equal_single_plan_calls(BT, dev, systems, precision):
     assert info["systems"] == 3
     assert info["near_items"] > 0 and info["far_items"] > 0
     og = info["orbitals_per_item"]
-    assert og == (8 if precision == "mixed" else 1)
+    assert og in ((4, 8, 16) if precision == "mixed" else (1,))
     Fs = [to_cuda(F)[0] for _, F, _, _ in systems]
     outs = S.convolve(Fs, Fs, [k for _, _, k, _ in systems], BT.Singularity.SUBTRACTION)
     for (mesh, F, k, plan), Ft, o in zip(systems, Fs, outs):

@@ -331,7 +331,7 @@ int tagi_orbitals_per_item(int kernel, int precision, int maxOrbitals, int reque
         return set_error(TAGI_ERR_ARG, "orbitalsPerItem %d must be 0 (automatic), 1, 4, 8 or 16", requested);
     if (maxOrbitals < 1 || degree < 1 || degree > MAX_DEGREE)
         return set_error(TAGI_ERR_ARG, "maxOrbitals %d, degree %d", maxOrbitals, degree);
-    *og = orbitals_per_item(kernel, precision, maxOrbitals, requested, degree + 1);
+    *og = orbitals_per_item(kernel, precision, &maxOrbitals, nullptr, 1, requested, degree + 1);
     return TAGI_OK;
 }
 

@@ -957,8 +957,10 @@ constexpr int KCHUNK16 = 32;
 // 64 orbital-pair updates, which hides its latency.  The per-orbital Kahan
 // sums live in shared memory (s_k[o][FT] sums, s_k[16 + o][FT]
 // compensations, touched once per KCHUNK16 sources), which leaves the
-// registers for the pipelined geometry.
-template <bool SS, bool MASK, bool PRECISE>
+// registers for the pipelined geometry.  NP: orbital pairs of the item that
+// hold orbitals (the last group of a request may be partly filled); the
+// pairs past NP are not computed.
+template <bool SS, bool MASK, bool PRECISE, int NP = 8>
 __device__ __forceinline__ void group16_tile(const float (*__restrict__ s)[GTILE], const float *__restrict__ s_q,
                                              int cnt4, float2 tx, float2 ty, float2 tz, float2 lx, float2 ly,
                                              float2 lz, const float2 (&nfi)[8], const float2 (&kc)[8],
@@ -1004,20 +1006,22 @@ __device__ __forceinline__ void group16_tile(const float (*__restrict__ s)[GTILE
             const float2 rd = dup2(ru), nd = dup2(nu), wd = dup2(wu);
             const float *qj = s_q + (j + u) * QS16;
 #pragma unroll
-            for (int o4 = 0; o4 < 4; o4++) {
+            for (int o4 = 0; o4 < (NP + 1) / 2; o4++) {
                 const float4 q4 = lds4(qj + 4 * o4);
 #pragma unroll
                 for (int h = 0; h < 2; h++) {
                     const int p = 2 * o4 + h;   // orbitals 2p, 2p+1
-                    const float2 q = h ? make_float2(q4.z, q4.w) : make_float2(q4.x, q4.y);
-                    const float2 g = ex2pos2(fma2(kc[p], rd, fma2(kl[p], rd, nd)));
-                    part[p] = fma2(g, SS ? fma2(nfi[p], wd, q) : q, part[p]);
+                    if (p < NP) {
+                        const float2 q = h ? make_float2(q4.z, q4.w) : make_float2(q4.x, q4.y);
+                        const float2 g = ex2pos2(fma2(kc[p], rd, fma2(kl[p], rd, nd)));
+                        part[p] = fma2(g, SS ? fma2(nfi[p], wd, q) : q, part[p]);
+                    }
                 }
             }
         }
         if ((j + 4) % KCHUNK16 == 0 || j + 4 >= cnt4) {   // end of a run of KCHUNK16 sources
 #pragma unroll
-            for (int p = 0; p < 8; p++) {
+            for (int p = 0; p < NP; p++) {
 #pragma unroll
                 for (int h = 0; h < 2; h++) {
                     const int o = 2 * p + h;
@@ -1037,6 +1041,29 @@ __device__ __forceinline__ void group16_tile(const float (*__restrict__ s)[GTILE
         }
     }
 }
+
+// group16_tile for the item's np filled orbital pairs (1..8).
+template <bool SS, bool MASK, bool PRECISE>
+__device__ __forceinline__ void group16_tile_np(int np, const float (*__restrict__ s)[GTILE],
+                                                const float *__restrict__ s_q, int cnt4, float2 tx, float2 ty,
+                                                float2 tz, float2 lx, float2 ly, float2 lz, const float2 (&nfi)[8],
+                                                const float2 (&kc)[8], const float2 (&kl)[8], float *__restrict__ s_k) {
+#define TAGI_G16(N) group16_tile<SS, MASK, PRECISE, N>(s, s_q, cnt4, tx, ty, tz, lx, ly, lz, nfi, kc, kl, s_k)
+    switch (np) {
+    case 1: TAGI_G16(1); break;
+    case 2: TAGI_G16(2); break;
+    case 3: TAGI_G16(3); break;
+    case 4: TAGI_G16(4); break;
+    case 5: TAGI_G16(5); break;
+    case 6: TAGI_G16(6); break;
+    case 7: TAGI_G16(7); break;
+    default: TAGI_G16(8); break;
+    }
+#undef TAGI_G16
+}
+
+// Filled orbital pairs of a 16-orbital item starting at orbital g0.
+__device__ __forceinline__ int group16_pairs(int norb, int g0) { return min(8, (norb - g0 + 1) >> 1); }
 
 // Per-orbital constants of a 16-orbital item, as orbital pairs.
 __device__ __forceinline__ void group16_constants(const Fields &a, int g0, float2 (&kc)[8], float2 (&kl)[8],
@@ -1151,10 +1178,12 @@ __global__ void __launch_bounds__(FT, 2) near_group16(const __grid_constant__ Wo
                     }
                     __syncthreads();
                     if (!warp_busy) continue;
+                    const int np = group16_pairs(a.norb, g0);
                     if (PASS == 1)
-                        group16_tile<SS, true, true>(s_src, s_q, cnt4, tx, ty, tz, lx, ly, lz, nfi, kc, kl, s_k);
+                        group16_tile_np<SS, true, true>(np, s_src, s_q, cnt4, tx, ty, tz, lx, ly, lz, nfi, kc, kl, s_k);
                     else
-                        group16_tile<SS, false, false>(s_src, s_q, cnt4, tx, ty, tz, lx, ly, lz, nfi, kc, kl, s_k);
+                        group16_tile_np<SS, false, false>(np, s_src, s_q, cnt4, tx, ty, tz, lx, ly, lz, nfi, kc, kl,
+                                                          s_k);
                 }
             }
             if (v) {
@@ -1169,7 +1198,8 @@ __global__ void __launch_bounds__(FT, 2) near_group16(const __grid_constant__ Wo
 
 // One staged proxy grid against one target for 16 orbitals (see far_cluster
 // for the padded innermost axis; charges staged QS16 floats per proxy point).
-template <bool SS, int MAXN1, bool EXACT>
+// NP: filled orbital pairs, as in group16_tile.
+template <bool SS, int MAXN1, bool EXACT, int NP = 8>
 __device__ __forceinline__ void far_group16_cluster(const float *__restrict__ s_q, const float *__restrict__ s_w,
                                                     const float (*s_p)[MAXN1], int n1_in, float tx, float ty,
                                                     float tz, const float2 (&nfi)[8], const float2 (&kc)[8],
@@ -1207,14 +1237,16 @@ __device__ __forceinline__ void far_group16_cluster(const float *__restrict__ s_
                         const float2 wd = dup2(u ? wk.y : wk.x);
                         const float *qk = s_q + (idx + 2 * m + u) * QS16;
 #pragma unroll
-                        for (int o4 = 0; o4 < 4; o4++) {
+                        for (int o4 = 0; o4 < (NP + 1) / 2; o4++) {
                             const float4 q4 = lds4(qk + 4 * o4);
 #pragma unroll
                             for (int h = 0; h < 2; h++) {
                                 const int p = 2 * o4 + h;
-                                const float2 q = h ? make_float2(q4.z, q4.w) : make_float2(q4.x, q4.y);
-                                const float2 g = ex2pos2(fma2(kc[p], rd, fma2(kl[p], rd, nd)));
-                                part[p] = fma2(g, SS ? fma2(nfi[p], wd, q) : q, part[p]);
+                                if (p < NP) {
+                                    const float2 q = h ? make_float2(q4.z, q4.w) : make_float2(q4.x, q4.y);
+                                    const float2 g = ex2pos2(fma2(kc[p], rd, fma2(kl[p], rd, nd)));
+                                    part[p] = fma2(g, SS ? fma2(nfi[p], wd, q) : q, part[p]);
+                                }
                             }
                         }
                     }
@@ -1223,11 +1255,31 @@ __device__ __forceinline__ void far_group16_cluster(const float *__restrict__ s_
             idx += n1p;
         }
 #pragma unroll
-        for (int p = 0; p < 8; p++) {
+        for (int p = 0; p < NP; p++) {
             kahan_add(sum[2 * p], cmp[2 * p], part[p].x);
             kahan_add(sum[2 * p + 1], cmp[2 * p + 1], part[p].y);
         }
     }
+}
+
+template <bool SS, int MAXN1, bool EXACT>
+__device__ __forceinline__ void far_group16_cluster_np(int np, const float *__restrict__ s_q,
+                                                       const float *__restrict__ s_w, const float (*s_p)[MAXN1],
+                                                       int n1, float tx, float ty, float tz, const float2 (&nfi)[8],
+                                                       const float2 (&kc)[8], const float2 (&kl)[8], float (&sum)[16],
+                                                       float (&cmp)[16]) {
+#define TAGI_F16(N) far_group16_cluster<SS, MAXN1, EXACT, N>(s_q, s_w, s_p, n1, tx, ty, tz, nfi, kc, kl, sum, cmp)
+    switch (np) {
+    case 1: TAGI_F16(1); break;
+    case 2: TAGI_F16(2); break;
+    case 3: TAGI_F16(3); break;
+    case 4: TAGI_F16(4); break;
+    case 5: TAGI_F16(5); break;
+    case 6: TAGI_F16(6); break;
+    case 7: TAGI_F16(7); break;
+    default: TAGI_F16(8); break;
+    }
+#undef TAGI_F16
 }
 
 // Dynamic shared memory of far_group16: charges (Pp * QS16 floats) then the
@@ -1304,7 +1356,8 @@ __global__ void __launch_bounds__(FT, 2) far_group16(const __grid_constant__ Wor
                 }
                 __syncthreads();
                 if (!warp_busy) continue;
-                far_group16_cluster<SS, MAXN1, EXACT>(s_q, s_w, s_p, n1, tx, ty, tz, nfi, kc, kl, sum, cmp);
+                far_group16_cluster_np<SS, MAXN1, EXACT>(group16_pairs(a.norb, g0), s_q, s_w, s_p, n1, tx, ty, tz,
+                                                         nfi, kc, kl, sum, cmp);
             }
             if (v) {
 #pragma unroll
@@ -2007,19 +2060,43 @@ int ensure_scratch(Plan &p, int norb) {
 }
 
 // Orbitals per work item: Yukawa in mixed precision shares each pair's
-// geometry across a group of 16, 8 or 4 orbitals once the largest system has
-// that many; everything else runs one orbital per item.  16 is taken up to
-// degree 7 (above it a 16-orbital proxy grid no longer fits two CTAs per SM)
-// when its padded orbital slots, at GROUP16_COST of a group-of-8 slot's time,
-// cost less than the group-of-8 slots.  requested > 0 (1, 4, 8 or 16)
-// overrides the choice where the kernel supports it.
-constexpr double GROUP16_COST = 0.86;
-int orbitals_per_item(int kernel, int precision, int max_norb, int requested, int max_n1) {
+// geometry across a group of 4, 8 or 16 orbitals; everything else (and fewer
+// than 4 orbitals) runs one orbital per item.  The choice minimises a cost
+// model measured on GB300 (1M-point mesh, degree 7): a pass over all batches
+// costs 1.0 per group of 8 (padded slots cost as much as filled ones), 0.59
+// per group of 4, and 0.345 + 0.18 np per group of 16 with np filled orbital
+// pairs (its kernels skip empty pairs); systems weigh by their point counts.
+// Groups of 16 only up to degree 7: above it a 16-orbital proxy grid no
+// longer fits two CTAs per SM.  requested > 0 (1, 4, 8 or 16) overrides the
+// choice where the kernel supports it.
+double group_cost(int og, int norb) {
+    if (og == 16) {
+        const int full = norb / 16, rem = norb % 16;
+        return full * (0.345 + 0.18 * 8) + (rem ? 0.345 + 0.18 * ((rem + 1) / 2) : 0.0);
+    }
+    if (og == 8) return 1.0 * ((norb + 7) / 8);
+    return 0.59 * ((norb + 3) / 4);
+}
+
+int orbitals_per_item(int kernel, int precision, const int *norb, const double *weight, int nsys, int requested,
+                      int max_n1) {
     if (kernel != KERNEL_YUKAWA || precision != PREC_MIXED) return 1;
     if (requested == 1 || requested == 4 || requested == 8 || requested == 16) return requested;
-    const double slots16 = 16.0 * ((max_norb + 15) / 16), slots8 = 8.0 * ((max_norb + 7) / 8);
-    if (max_norb >= 16 && max_n1 <= 8 && GROUP16_COST * slots16 < slots8) return 16;
-    return max_norb >= 8 ? 8 : (max_norb >= 4 ? 4 : 1);
+    int maxo = 0;
+    for (int i = 0; i < nsys; i++) maxo = norb[i] > maxo ? norb[i] : maxo;
+    if (maxo < 4) return 1;
+    int best = 0;
+    double best_cost = 0.0;
+    for (int og : {4, 8, 16}) {
+        if (og == 16 && max_n1 > 8) continue;
+        double c = 0.0;
+        for (int i = 0; i < nsys; i++) c += (weight ? weight[i] : 1.0) * group_cost(og, norb[i]);
+        if (!best || c < best_cost) {
+            best = og;
+            best_cost = c;
+        }
+    }
+    return best;
 }
 
 bool schedule_matches(const Schedule &sc, const int *norb, int nsys, int og) {
@@ -2170,7 +2247,7 @@ int convolve_systems(SysCall *calls, int nsys, int kernel, int singularity, int 
 int convolve(Plan &p, const double *tv, const double *sv, double *out, int norb, int kernel,
              const double *kparams, int nkp, int singularity, int precision, cudaStream_t s, bool kp_device,
              int og_request, int nt_request) {
-    const int og = orbitals_per_item(kernel, precision, norb, og_request, p.n1);
+    const int og = orbitals_per_item(kernel, precision, &norb, nullptr, 1, og_request, p.n1);
     const Schedule *sc = nullptr;
     for (const Schedule &c : p.scheds)
         if (schedule_matches(c, &norb, 1, og)) sc = &c;

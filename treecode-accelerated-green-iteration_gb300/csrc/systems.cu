@@ -119,8 +119,12 @@ int tagi_systems_create(tagi_systems **systems, int numSystems, tagi_plan *const
         y->norb.push_back(numOrbitals[i]);
     }
     int maxn1 = 0;
-    for (Plan *q : y->plans) maxn1 = q->n1 > maxn1 ? q->n1 : maxn1;
-    const int og = orbitals_per_item(kernel, precision, maxo, orbitalsPerItem, maxn1);
+    std::vector<double> wt;
+    for (Plan *q : y->plans) {
+        maxn1 = q->n1 > maxn1 ? q->n1 : maxn1;
+        wt.push_back((double)q->src.n);
+    }
+    const int og = orbitals_per_item(kernel, precision, y->norb.data(), wt.data(), numSystems, orbitalsPerItem, maxn1);
     int rc = build_schedule(y->plans.data(), y->norb.data(), numSystems, og, y->sched, y->stream);
     if (!rc) {
         void *v = nullptr;

@@ -227,7 +227,8 @@ int modified_charges(Plan &p, int precision, int norb, cudaStream_t s);
 // fields.cu
 constexpr int MAX_SYSTEMS = 8;  // systems per field launch
 int ensure_scratch(Plan &p, int norb);
-int orbitals_per_item(int kernel, int precision, int max_norb, int requested, int max_n1);
+int orbitals_per_item(int kernel, int precision, const int *norb, const double *weight, int nsys, int requested,
+                      int max_n1);
 int build_schedule(Plan *const *plans, const int *norb, int nsys, int og, Schedule &sc, cudaStream_t s);
 bool schedule_matches(const Schedule &sc, const int *norb, int nsys, int og);
 int convolve_systems(SysCall *calls, int nsys, int kernel, int singularity, int precision,
