@@ -82,9 +82,9 @@ CPU_SAMPLE_BATCHES = 48  # stratified target batches per CPU-baseline sample
 #   far_mixed   r^2 from per-axis squares (1 + 2/n1 for the row sums), then as
 #               the near loop
 #   near_group  per pair 3 + 3 + r + (-log2 r) (shared by OG orbitals, one
-#               rsqrt and one lg2); per orbital the split exponent with the
-#               -log2 r folded in (2), q - f_i w, accumulate
-#   far_group   per pair r^2 + r + (-log2 r) (+ 2/n1); per orbital 4
+#               rsqrt and one lg2); per orbital the exponent -k log2(e) r with
+#               the -log2 r folded in (1), q - f_i w, accumulate
+#   far_group   per pair r^2 + r + (-log2 r) (+ 2/n1); per orbital 3
 # Returned as (FP32 lane ops, MUFU ex2, MUFU rsqrt, MUFU lg2) per unit.
 def field_ops(kernel, label, og=8, n1=8):
     yuk = label.startswith("yukawa")
@@ -93,9 +93,9 @@ def field_ops(kernel, label, og=8, n1=8):
     if kernel == "far_mixed":
         return (5.0 + 2.0 / n1, 1.0, 1.0, 0.0) if yuk else (4.0 + 2.0 / n1, 1.0, 1.0, 0.0)
     if kernel == "near_group":
-        return (4.0 + 8.0 / og, 1.0, 1.0 / og, 1.0 / og)
+        return (3.0 + 8.0 / og, 1.0, 1.0 / og, 1.0 / og)
     if kernel == "far_group":
-        return (4.0 + (3.0 + 2.0 / n1) / og, 1.0, 1.0 / og, 1.0 / og)
+        return (3.0 + (3.0 + 2.0 / n1) / og, 1.0, 1.0 / og, 1.0 / og)
     raise ValueError(kernel)
 
 

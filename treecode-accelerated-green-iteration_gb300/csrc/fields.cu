@@ -233,11 +233,6 @@ __device__ __forceinline__ void near_tile(const float (*__restrict__ s)[NTILE], 
     }
 }
 
-// Split an FP64 value into FP32 hi + lo.
-__device__ __forceinline__ void split_f32(double v, float &hi, float &lo) {
-    hi = (float)v;
-    lo = (float)(v - (double)hi);
-}
 
 // ---------------------------------------------------------------------------
 // Near field, mixed precision.
@@ -534,7 +529,7 @@ template <bool SS, bool MASK, bool PRECISE, int OG>
 __device__ __forceinline__ void group_tile(const float (*__restrict__ s)[GTILE], const float4 *__restrict__ s_q4,
                                            int cnt2, float2 tx, float2 ty, float2 tz, float2 lx, float2 ly,
                                            float2 lz, const float2 (&nfi)[OG], const float2 (&kc)[OG],
-                                           const float2 (&kl)[OG], float (&sum)[OG], float (&cmp)[OG]) {
+                                           float (&sum)[OG], float (&cmp)[OG]) {
     for (int j0 = 0; j0 < cnt2; j0 += KCHUNK) {
         const int j1 = min(j0 + KCHUNK, cnt2);
         float2 part[OG];
@@ -567,7 +562,7 @@ __device__ __forceinline__ void group_tile(const float (*__restrict__ s)[GTILE],
                     const int o = 2 * o2 + u;
                     const float2 q = u ? make_float2(q4.z, q4.w) : make_float2(q4.x, q4.y);
                     // e^{-k r} / r = 2^{-k log2(e) r - log2 r}, the constant split hi + lo
-                    const float2 g = ex2pos2(fma2(kc[o], r, fma2(kl[o], r, nl)));
+                    const float2 g = ex2pos2(fma2(kc[o], r, nl));
                     part[o] = fma2(g, SS ? fma2(nfi[o], wv, q) : q, part[o]);
                 }
             }
@@ -593,16 +588,12 @@ __global__ void __launch_bounds__(FT, 2) near_group(const __grid_constant__ Work
         const int bn = a.batch_node[b];
         const int tb = a.tbegin[bn], te = a.tend[bn];
         const double cbx = a.tcenter[3L * bn], cby = a.tcenter[3L * bn + 1], cbz = a.tcenter[3L * bn + 2];
-        float2 kc[OG], kl[OG];
+        float2 kc[OG];
         float kmin = 3.4e38f;
 #pragma unroll
         for (int o = 0; o < OG; o++) {
             const int orb = g0 + o;
-            const double k2 = orb < a.norb ? -a.kp64[orb] * LOG2E : 0.0;   // -k log2(e)
-            float h, l;
-            split_f32(k2, h, l);
-            kc[o] = dup2(h);
-            kl[o] = dup2(l);
+            kc[o] = dup2(orb < a.norb ? -a.kc32[orb] : 0.f);   // -k log2(e) as one FP32 constant
             if (orb < a.norb) kmin = fminf(kmin, a.kc32[orb]);
         }
         const int r0 = a.rng_off[b], r1 = a.rng_off[b + 1];
@@ -671,10 +662,10 @@ __global__ void __launch_bounds__(FT, 2) near_group(const __grid_constant__ Work
                     __syncthreads();
                     if (!warp_busy) continue;
                     if (PASS == 1)
-                        group_tile<SS, true, true, OG>(s_src, s_q4, cnt2, tx, ty, tz, lx, ly, lz, nfi, kc, kl, sum,
+                        group_tile<SS, true, true, OG>(s_src, s_q4, cnt2, tx, ty, tz, lx, ly, lz, nfi, kc, sum,
                                                        cmp);
                     else
-                        group_tile<SS, false, false, OG>(s_src, s_q4, cnt2, tx, ty, tz, lx, ly, lz, nfi, kc, kl, sum,
+                        group_tile<SS, false, false, OG>(s_src, s_q4, cnt2, tx, ty, tz, lx, ly, lz, nfi, kc, sum,
                                                          cmp);
                 }
             }
@@ -693,7 +684,7 @@ template <bool SS, int MAXN1, int OG, bool EXACT = false>
 __device__ __forceinline__ void far_group_cluster(const float4 *__restrict__ s_q4, const float *__restrict__ s_w,
                                                   const float (*s_p)[MAXN1], int n1_in, float tx, float ty, float tz,
                                                   const float2 (&nfi)[OG], const float2 (&kc)[OG],
-                                                  const float2 (&kl)[OG], float (&sum)[OG], float (&cmp)[OG]) {
+                                                  float (&sum)[OG], float (&cmp)[OG]) {
     constexpr int MH = even_up<MAXN1>() / 2;
     const int n1 = EXACT ? MAXN1 : n1_in;
     const int n1p = n1 + (n1 & 1);
@@ -728,7 +719,7 @@ __device__ __forceinline__ void far_group_cluster(const float4 *__restrict__ s_q
                         for (int u = 0; u < 2; u++) {
                             const int o = 2 * o2 + u;
                             const float2 q = u ? make_float2(q4.z, q4.w) : make_float2(q4.x, q4.y);
-                            const float2 g = ex2pos2(fma2(kc[o], rr, fma2(kl[o], rr, nl)));
+                            const float2 g = ex2pos2(fma2(kc[o], rr, nl));
                             part[o] = fma2(g, SS ? fma2(nfi[o], wk, q) : q, part[o]);
                         }
                     }
@@ -769,14 +760,9 @@ __global__ void __launch_bounds__(FT, 2) far_group(const __grid_constant__ Work 
         const int bn = a.batch_node[b];
         const int tb = a.tbegin[bn], te = a.tend[bn];
         const double cb[3] = {a.tcenter[3L * bn], a.tcenter[3L * bn + 1], a.tcenter[3L * bn + 2]};
-        float2 kc[OG], kl[OG];
+        float2 kc[OG];
 #pragma unroll
-        for (int o = 0; o < OG; o++) {
-            float h, l;
-            split_f32((g0 + o) < a.norb ? -a.kp64[g0 + o] * LOG2E : 0.0, h, l);
-            kc[o] = dup2(h);
-            kl[o] = dup2(l);
-        }
+        for (int o = 0; o < OG; o++) kc[o] = dup2((g0 + o) < a.norb ? -a.kc32[g0 + o] : 0.f);
         for (int base = tb; base < te; base += FT) {
             const int i = base + tid;
             const bool v = i < te;
@@ -815,7 +801,7 @@ __global__ void __launch_bounds__(FT, 2) far_group(const __grid_constant__ Work 
                 }
                 __syncthreads();
                 if (!warp_busy) continue;
-                far_group_cluster<SS, MAXN1, OG, EXACT>(s_q4, s_w, s_p, n1, tx, ty, tz, nfi, kc, kl, sum, cmp);
+                far_group_cluster<SS, MAXN1, OG, EXACT>(s_q4, s_w, s_p, n1, tx, ty, tz, nfi, kc, sum, cmp);
             }
             if (v) {
 #pragma unroll
@@ -867,14 +853,9 @@ __global__ void __launch_bounds__(FT, 2) far_group_db(const __grid_constant__ Wo
         const int bn = a.batch_node[b];
         const int tb = a.tbegin[bn], te = a.tend[bn];
         const double cb[3] = {a.tcenter[3L * bn], a.tcenter[3L * bn + 1], a.tcenter[3L * bn + 2]};
-        float2 kc[OG], kl[OG];
+        float2 kc[OG];
 #pragma unroll
-        for (int o = 0; o < OG; o++) {
-            float h, l;
-            split_f32((g0 + o) < a.norb ? -a.kp64[g0 + o] * LOG2E : 0.0, h, l);
-            kc[o] = dup2(h);
-            kl[o] = dup2(l);
-        }
+        for (int o = 0; o < OG; o++) kc[o] = dup2((g0 + o) < a.norb ? -a.kc32[g0 + o] : 0.f);
         // issue the copies of far cluster e into buffer buf (completes at the next wait + barrier)
         auto stage = [&](int e, int buf) {
             const int slot = a.node_slot[a.far_list[e]];
@@ -921,7 +902,7 @@ __global__ void __launch_bounds__(FT, 2) far_group_db(const __grid_constant__ Wo
                 if (!warp_busy) continue;
                 const float *q = s_dyn + (size_t)cur * BUF;
                 far_group_cluster<SS, DB_N1, OG, true>(reinterpret_cast<const float4 *>(q), q + DB_P * OG, s_p[cur],
-                                                       DB_N1, tx, ty, tz, nfi, kc, kl, sum, cmp);
+                                                       DB_N1, tx, ty, tz, nfi, kc, sum, cmp);
             }
             if (v) {
 #pragma unroll
@@ -964,7 +945,7 @@ template <bool SS, bool MASK, bool PRECISE, int NP = 8>
 __device__ __forceinline__ void group16_tile(const float (*__restrict__ s)[GTILE], const float *__restrict__ s_q,
                                              int cnt4, float2 tx, float2 ty, float2 tz, float2 lx, float2 ly,
                                              float2 lz, const float2 (&nfi)[8], const float2 (&kc)[8],
-                                             const float2 (&kl)[8], float *__restrict__ s_k) {
+                                             float *__restrict__ s_k) {
     // r, -log2 r and w of the source pair at j (packed over the two sources)
     auto geometry = [&](int j, float2 &r, float2 &nl, float2 &wv) {
         float2 dx = add2(tx, lds2(s[0] + j)), dy = add2(ty, lds2(s[1] + j)), dz = add2(tz, lds2(s[2] + j));
@@ -1013,7 +994,7 @@ __device__ __forceinline__ void group16_tile(const float (*__restrict__ s)[GTILE
                     const int p = 2 * o4 + h;   // orbitals 2p, 2p+1
                     if (p < NP) {
                         const float2 q = h ? make_float2(q4.z, q4.w) : make_float2(q4.x, q4.y);
-                        const float2 g = ex2pos2(fma2(kc[p], rd, fma2(kl[p], rd, nd)));
+                        const float2 g = ex2pos2(fma2(kc[p], rd, nd));
                         part[p] = fma2(g, SS ? fma2(nfi[p], wd, q) : q, part[p]);
                     }
                 }
@@ -1047,8 +1028,8 @@ template <bool SS, bool MASK, bool PRECISE>
 __device__ __forceinline__ void group16_tile_np(int np, const float (*__restrict__ s)[GTILE],
                                                 const float *__restrict__ s_q, int cnt4, float2 tx, float2 ty,
                                                 float2 tz, float2 lx, float2 ly, float2 lz, const float2 (&nfi)[8],
-                                                const float2 (&kc)[8], const float2 (&kl)[8], float *__restrict__ s_k) {
-#define TAGI_G16(N) group16_tile<SS, MASK, PRECISE, N>(s, s_q, cnt4, tx, ty, tz, lx, ly, lz, nfi, kc, kl, s_k)
+                                                const float2 (&kc)[8], float *__restrict__ s_k) {
+#define TAGI_G16(N) group16_tile<SS, MASK, PRECISE, N>(s, s_q, cnt4, tx, ty, tz, lx, ly, lz, nfi, kc, s_k)
     switch (np) {
     case 1: TAGI_G16(1); break;
     case 2: TAGI_G16(2); break;
@@ -1066,17 +1047,12 @@ __device__ __forceinline__ void group16_tile_np(int np, const float (*__restrict
 __device__ __forceinline__ int group16_pairs(int norb, int g0) { return min(8, (norb - g0 + 1) >> 1); }
 
 // Per-orbital constants of a 16-orbital item, as orbital pairs.
-__device__ __forceinline__ void group16_constants(const Fields &a, int g0, float2 (&kc)[8], float2 (&kl)[8],
-                                                  float *kmin) {
+__device__ __forceinline__ void group16_constants(const Fields &a, int g0, float2 (&kc)[8], float *kmin) {
     float km = 3.4e38f;
 #pragma unroll
     for (int p = 0; p < 8; p++) {
-        float h0, l0, h1, l1;
         const int o0 = g0 + 2 * p, o1 = o0 + 1;
-        split_f32(o0 < a.norb ? -a.kp64[o0] * LOG2E : 0.0, h0, l0);   // -k log2(e)
-        split_f32(o1 < a.norb ? -a.kp64[o1] * LOG2E : 0.0, h1, l1);
-        kc[p] = make_float2(h0, h1);
-        kl[p] = make_float2(l0, l1);
+        kc[p] = make_float2(o0 < a.norb ? -a.kc32[o0] : 0.f, o1 < a.norb ? -a.kc32[o1] : 0.f);   // -k log2(e)
         if (o0 < a.norb) km = fminf(km, a.kc32[o0]);
         if (o1 < a.norb) km = fminf(km, a.kc32[o1]);
     }
@@ -1107,9 +1083,9 @@ __global__ void __launch_bounds__(FT, 2) near_group16(const __grid_constant__ Wo
         const int bn = a.batch_node[b];
         const int tb = a.tbegin[bn], te = a.tend[bn];
         const double cbx = a.tcenter[3L * bn], cby = a.tcenter[3L * bn + 1], cbz = a.tcenter[3L * bn + 2];
-        float2 kc[8], kl[8];
+        float2 kc[8];
         float kmin;
-        group16_constants(a, g0, kc, kl, &kmin);
+        group16_constants(a, g0, kc, &kmin);
         const int r0 = a.rng_off[b], r1 = a.rng_off[b + 1];
         for (int base = tb; base < te; base += FT) {
             const int i = base + tid;
@@ -1180,9 +1156,9 @@ __global__ void __launch_bounds__(FT, 2) near_group16(const __grid_constant__ Wo
                     if (!warp_busy) continue;
                     const int np = group16_pairs(a.norb, g0);
                     if (PASS == 1)
-                        group16_tile_np<SS, true, true>(np, s_src, s_q, cnt4, tx, ty, tz, lx, ly, lz, nfi, kc, kl, s_k);
+                        group16_tile_np<SS, true, true>(np, s_src, s_q, cnt4, tx, ty, tz, lx, ly, lz, nfi, kc, s_k);
                     else
-                        group16_tile_np<SS, false, false>(np, s_src, s_q, cnt4, tx, ty, tz, lx, ly, lz, nfi, kc, kl,
+                        group16_tile_np<SS, false, false>(np, s_src, s_q, cnt4, tx, ty, tz, lx, ly, lz, nfi, kc,
                                                           s_k);
                 }
             }
@@ -1203,7 +1179,7 @@ template <bool SS, int MAXN1, bool EXACT, int NP = 8>
 __device__ __forceinline__ void far_group16_cluster(const float *__restrict__ s_q, const float *__restrict__ s_w,
                                                     const float (*s_p)[MAXN1], int n1_in, float tx, float ty,
                                                     float tz, const float2 (&nfi)[8], const float2 (&kc)[8],
-                                                    const float2 (&kl)[8], float (&sum)[16], float (&cmp)[16]) {
+                                                    float (&sum)[16], float (&cmp)[16]) {
     constexpr int MH = even_up<MAXN1>() / 2;
     const int n1 = EXACT ? MAXN1 : n1_in;
     const int n1p = n1 + (n1 & 1);
@@ -1244,7 +1220,7 @@ __device__ __forceinline__ void far_group16_cluster(const float *__restrict__ s_
                                 const int p = 2 * o4 + h;
                                 if (p < NP) {
                                     const float2 q = h ? make_float2(q4.z, q4.w) : make_float2(q4.x, q4.y);
-                                    const float2 g = ex2pos2(fma2(kc[p], rd, fma2(kl[p], rd, nd)));
+                                    const float2 g = ex2pos2(fma2(kc[p], rd, nd));
                                     part[p] = fma2(g, SS ? fma2(nfi[p], wd, q) : q, part[p]);
                                 }
                             }
@@ -1266,9 +1242,9 @@ template <bool SS, int MAXN1, bool EXACT>
 __device__ __forceinline__ void far_group16_cluster_np(int np, const float *__restrict__ s_q,
                                                        const float *__restrict__ s_w, const float (*s_p)[MAXN1],
                                                        int n1, float tx, float ty, float tz, const float2 (&nfi)[8],
-                                                       const float2 (&kc)[8], const float2 (&kl)[8], float (&sum)[16],
+                                                       const float2 (&kc)[8], float (&sum)[16],
                                                        float (&cmp)[16]) {
-#define TAGI_F16(N) far_group16_cluster<SS, MAXN1, EXACT, N>(s_q, s_w, s_p, n1, tx, ty, tz, nfi, kc, kl, sum, cmp)
+#define TAGI_F16(N) far_group16_cluster<SS, MAXN1, EXACT, N>(s_q, s_w, s_p, n1, tx, ty, tz, nfi, kc, sum, cmp)
     switch (np) {
     case 1: TAGI_F16(1); break;
     case 2: TAGI_F16(2); break;
@@ -1309,8 +1285,8 @@ __global__ void __launch_bounds__(FT, 2) far_group16(const __grid_constant__ Wor
         const int bn = a.batch_node[b];
         const int tb = a.tbegin[bn], te = a.tend[bn];
         const double cb[3] = {a.tcenter[3L * bn], a.tcenter[3L * bn + 1], a.tcenter[3L * bn + 2]};
-        float2 kc[8], kl[8];
-        group16_constants(a, g0, kc, kl, nullptr);
+        float2 kc[8];
+        group16_constants(a, g0, kc, nullptr);
         for (int base = tb; base < te; base += FT) {
             const int i = base + tid;
             const bool v = i < te;
@@ -1357,7 +1333,7 @@ __global__ void __launch_bounds__(FT, 2) far_group16(const __grid_constant__ Wor
                 __syncthreads();
                 if (!warp_busy) continue;
                 far_group16_cluster_np<SS, MAXN1, EXACT>(group16_pairs(a.norb, g0), s_q, s_w, s_p, n1, tx, ty, tz,
-                                                         nfi, kc, kl, sum, cmp);
+                                                         nfi, kc, sum, cmp);
             }
             if (v) {
 #pragma unroll
@@ -1646,20 +1622,17 @@ __global__ void __launch_bounds__(FT, 2) pair_peak_near_group(int reps, float *o
     for (int k = threadIdx.x; k < GTILE * OG; k += FT) reinterpret_cast<float *>(s_q4)[k] = 0.5f + 0.001f * k;
     __syncthreads();
     const float2 tx = dup2(0.01f * (threadIdx.x & 31)), ty = dup2(0.02f), tz = dup2(-0.03f * (threadIdx.x >> 5));
-    float2 nfi[OG], kc[OG], kl[OG];
+    float2 nfi[OG], kc[OG];
     float sum[OG], cmp[OG];
 #pragma unroll
     for (int o = 0; o < OG; o++) {
-        float h, l;
-        split_f32(-(0.5 + 0.3 * o) * LOG2E, h, l);
-        kc[o] = dup2(h);
-        kl[o] = dup2(l);
+        kc[o] = dup2((float)(-(0.5 + 0.3 * o) * LOG2E));
         nfi[o] = dup2(-0.3f);
         sum[o] = cmp[o] = 0.f;
     }
     const float2 z = dup2(0.f);
     for (int r = 0; r < reps; r++)
-        group_tile<SS, false, false, OG>(s, s_q4, GTILE, tx, ty, tz, z, z, z, nfi, kc, kl, sum, cmp);
+        group_tile<SS, false, false, OG>(s, s_q4, GTILE, tx, ty, tz, z, z, z, nfi, kc, sum, cmp);
     float acc = 0.f;
 #pragma unroll
     for (int o = 0; o < OG; o++) acc += sum[o] - cmp[o];
@@ -1678,19 +1651,16 @@ __global__ void __launch_bounds__(FT, 2) pair_peak_far_group(int reps, float *ou
     if (threadIdx.x < 3 * N1) s_p[threadIdx.x / N1][threadIdx.x % N1] = 1.0f + 0.1f * threadIdx.x;
     __syncthreads();
     const float tx = 0.01f * (threadIdx.x & 31), ty = 0.02f, tz = -0.03f * (threadIdx.x >> 5);
-    float2 nfi[OG], kc[OG], kl[OG];
+    float2 nfi[OG], kc[OG];
     float sum[OG], cmp[OG];
 #pragma unroll
     for (int o = 0; o < OG; o++) {
-        float h, l;
-        split_f32(-(0.5 + 0.3 * o) * LOG2E, h, l);
-        kc[o] = dup2(h);
-        kl[o] = dup2(l);
+        kc[o] = dup2((float)(-(0.5 + 0.3 * o) * LOG2E));
         nfi[o] = dup2(-0.3f);
         sum[o] = cmp[o] = 0.f;
     }
     for (int r = 0; r < reps; r++)
-        far_group_cluster<SS, N1, OG, true>(s_q4, s_w, s_p, N1, tx, ty, tz, nfi, kc, kl, sum, cmp);
+        far_group_cluster<SS, N1, OG, true>(s_q4, s_w, s_p, N1, tx, ty, tz, nfi, kc, sum, cmp);
     float acc = 0.f;
 #pragma unroll
     for (int o = 0; o < OG; o++) acc += sum[o] - cmp[o];
@@ -1716,20 +1686,16 @@ __global__ void __launch_bounds__(FT, 2) pair_peak_near_group16(int reps, float 
     for (int k = threadIdx.x; k < PEAK16_TILE * QS16; k += FT) s_q[k] = 0.5f + 0.001f * k;
     __syncthreads();
     const float2 tx = dup2(0.01f * (threadIdx.x & 31)), ty = dup2(0.02f), tz = dup2(-0.03f * (threadIdx.x >> 5));
-    float2 nfi[8], kc[8], kl[8];
+    float2 nfi[8], kc[8];
 #pragma unroll
     for (int p = 0; p < 8; p++) {
-        float h0, l0, h1, l1;
-        split_f32(-(0.5 + 0.3 * (2 * p)) * LOG2E, h0, l0);
-        split_f32(-(0.5 + 0.3 * (2 * p + 1)) * LOG2E, h1, l1);
-        kc[p] = make_float2(h0, h1);
-        kl[p] = make_float2(l0, l1);
+        kc[p] = make_float2((float)(-(0.5 + 0.3 * (2 * p)) * LOG2E), (float)(-(0.5 + 0.3 * (2 * p + 1)) * LOG2E));
         nfi[p] = dup2(-0.3f);
     }
     for (int o = 0; o < 32; o++) s_k[o * FT + threadIdx.x] = 0.f;
     const float2 z = dup2(0.f);
     for (int r = 0; r < reps; r++)
-        group16_tile<SS, false, false>(s, s_q, PEAK16_TILE, tx, ty, tz, z, z, z, nfi, kc, kl, s_k);
+        group16_tile<SS, false, false>(s, s_q, PEAK16_TILE, tx, ty, tz, z, z, z, nfi, kc, s_k);
     float acc = 0.f;
     for (int o = 0; o < 16; o++) acc += s_k[o * FT + threadIdx.x] - s_k[(16 + o) * FT + threadIdx.x];
     out[blockIdx.x * FT + threadIdx.x] = acc;
@@ -1746,21 +1712,17 @@ __global__ void __launch_bounds__(FT, 2) pair_peak_far_group16(int reps, float *
     if (threadIdx.x < 3 * N1) s_p[threadIdx.x / N1][threadIdx.x % N1] = 1.0f + 0.1f * threadIdx.x;
     __syncthreads();
     const float tx = 0.01f * (threadIdx.x & 31), ty = 0.02f, tz = -0.03f * (threadIdx.x >> 5);
-    float2 nfi[8], kc[8], kl[8];
+    float2 nfi[8], kc[8];
     float sum[16], cmp[16];
 #pragma unroll
     for (int p = 0; p < 8; p++) {
-        float h0, l0, h1, l1;
-        split_f32(-(0.5 + 0.3 * (2 * p)) * LOG2E, h0, l0);
-        split_f32(-(0.5 + 0.3 * (2 * p + 1)) * LOG2E, h1, l1);
-        kc[p] = make_float2(h0, h1);
-        kl[p] = make_float2(l0, l1);
+        kc[p] = make_float2((float)(-(0.5 + 0.3 * (2 * p)) * LOG2E), (float)(-(0.5 + 0.3 * (2 * p + 1)) * LOG2E));
         nfi[p] = dup2(-0.3f);
     }
 #pragma unroll
     for (int o = 0; o < 16; o++) sum[o] = cmp[o] = 0.f;
     for (int r = 0; r < reps; r++)
-        far_group16_cluster<SS, N1, true>(s_q, s_w, s_p, N1, tx, ty, tz, nfi, kc, kl, sum, cmp);
+        far_group16_cluster<SS, N1, true>(s_q, s_w, s_p, N1, tx, ty, tz, nfi, kc, sum, cmp);
     float acc = 0.f;
 #pragma unroll
     for (int o = 0; o < 16; o++) acc += sum[o] - cmp[o];
@@ -1946,9 +1908,15 @@ int launch_fields(const SysCall *calls, const Fields *f, int nsys, const Schedul
 // d_ss = subtraction factor 4 pi/k^2 (Yukawa) or 2 pi/a^2 (Coulomb), 0
 // without subtraction.  A parameter the kernel cannot use sets bit 0 of err
 // and makes the orbital's subtraction factor NaN, so all its outputs are NaN.
+// Mixed precision: the field kernels see k only through the FP32 constant sc
+// (k log2(e), or a sqrt(log2(e))), so the subtraction factor uses the k that
+// sc represents exactly, k' = sc / log2(e) (a' = sc / sqrt(log2(e))): sums and
+// subtraction term then belong to one kernel parameter, k' = k (1 + O(2^-24)),
+// and the rounding of k moves the result by about twice that, smoothly,
+// instead of entering the cancellation of the subtraction.
 __global__ void orbital_constants(const double *__restrict__ kp, int nkp, int norb, int kernel, int sing,
-                                  double *__restrict__ kpo, float *__restrict__ kc, double *__restrict__ ss,
-                                  int *__restrict__ err) {
+                                  int mixed, double *__restrict__ kpo, float *__restrict__ kc,
+                                  double *__restrict__ ss, int *__restrict__ err) {
     const int o = blockIdx.x * blockDim.x + threadIdx.x;
     if (o >= norb) return;
     const double k = kp[(long)o * nkp];
@@ -1961,7 +1929,10 @@ __global__ void orbital_constants(const double *__restrict__ kp, int nkp, int no
     else if (sing == SING_SUBTRACTION) c = (float)(k * sqrt(LOG2E));
     kc[o] = c;
     double f = 0.0;
-    if (sing == SING_SUBTRACTION) f = (kernel == KERNEL_YUKAWA ? 4.0 : 2.0) * M_PI / (k * k);
+    double ke = k;
+    if (mixed && kernel == KERNEL_YUKAWA) ke = (double)c / LOG2E;
+    else if (mixed && sing == SING_SUBTRACTION) ke = (double)c / sqrt(LOG2E);
+    if (sing == SING_SUBTRACTION) f = (kernel == KERNEL_YUKAWA ? 4.0 : 2.0) * M_PI / (ke * ke);
     ss[o] = bad ? __longlong_as_double(0x7ff8000000000000LL) : f;  // NaN marks every output of the orbital
 }
 
@@ -2153,7 +2124,7 @@ int build_schedule(Plan *const *plans, const int *norb, int nsys, int og, Schedu
 }
 
 // Per-orbital constants of one system into p.d_kp / d_kc / d_ss.
-static int orbital_setup(Plan &p, const SysCall &c, int kernel, int singularity, cudaStream_t s) {
+static int orbital_setup(Plan &p, const SysCall &c, int kernel, int singularity, int mixed, cudaStream_t s) {
     const double *src = c.kp;
     int stride = c.nkp;
     if (!c.kp_device) {
@@ -2163,8 +2134,8 @@ static int orbital_setup(Plan &p, const SysCall &c, int kernel, int singularity,
         src = p.d_kp;
         stride = 1;
     }
-    launch(orbital_constants, (c.norb + 127) / 128, 128, 0, s, src, stride, c.norb, kernel, singularity, p.d_kp,
-           p.d_kc, p.d_ss, p.err_flag + 1);
+    launch(orbital_constants, (c.norb + 127) / 128, 128, 0, s, src, stride, c.norb, kernel, singularity, mixed,
+           p.d_kp, p.d_kc, p.d_ss, p.err_flag + 1);
     TAGI_LAUNCH_CHECK();
     return TAGI_OK;
 }
@@ -2194,7 +2165,7 @@ int convolve_systems(SysCall *calls, int nsys, int kernel, int singularity, int 
                                  "precision, and kernel parameters on the device");
         }
         TAGI_TRY(ensure_scratch(p, c.norb));
-        TAGI_TRY(orbital_setup(p, c, kernel, singularity, s));
+        TAGI_TRY(orbital_setup(p, c, kernel, singularity, mixed ? 1 : 0, s));
         const int ns = p.src.n, nt = p.tgt.n;
         dim3 gs((ns + 255) / 256, c.norb), gt((nt + 255) / 256, c.norb);
         phase_mark(PH_GLUE, true, s);
