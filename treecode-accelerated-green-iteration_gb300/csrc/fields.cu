@@ -509,9 +509,11 @@ __global__ void __launch_bounds__(FT, 2) far_mixed(const __grid_constant__ Work 
 // OG orbitals).  Per two sources (or two proxy points) the differences, r^2,
 // r (via rsqrt) and -log2 r (via lg2) are formed once for the group in packed
 // operations; each orbital then adds 2^{-k_o log2(e) r - log2 r} * c, which is
-// e^{-k_o r} / r * c with the 1/r folded into the exponent (the constant
-// -k_o log2(e) split hi + lo).  Coordinates are translated to the batch center but not
-// scaled (each orbital has its own k).  Charges are staged as float4
+// e^{-k_o r} / r * c with the 1/r folded into the exponent.  -k_o log2(e) is
+// the orbital's FP32 constant sc (orbital_constants), and the subtraction term
+// uses the k that sc represents, so one FP32 constant suffices.  Coordinates
+// are translated to the batch center but not scaled (each orbital has its own
+// k).  Charges are staged as float4
 // {q(o, j), q(o, j+1), q(o+1, j), q(o+1, j+1)} per (pair of sources, pair of
 // orbitals), so one 16-byte shared read serves four (pair, orbital) terms.
 // Orbitals past the last one of the request have zero charges and are not
@@ -561,7 +563,7 @@ __device__ __forceinline__ void group_tile(const float (*__restrict__ s)[GTILE],
                 for (int u = 0; u < 2; u++) {
                     const int o = 2 * o2 + u;
                     const float2 q = u ? make_float2(q4.z, q4.w) : make_float2(q4.x, q4.y);
-                    // e^{-k r} / r = 2^{-k log2(e) r - log2 r}, the constant split hi + lo
+                    // e^{-k r} / r = 2^{-k log2(e) r - log2 r}
                     const float2 g = ex2pos2(fma2(kc[o], r, nl));
                     part[o] = fma2(g, SS ? fma2(nfi[o], wv, q) : q, part[o]);
                 }
@@ -916,9 +918,9 @@ __global__ void __launch_bounds__(FT, 2) far_group_db(const __grid_constant__ Wo
 // ---------------------------------------------------------------------------
 // Orbital-group kernels with 16 orbitals per item, packed by ORBITAL: the two
 // lanes of every packed operation are orbitals (2p, 2p+1) of one source (or
-// proxy point).  The per-orbital constants -k log2(e) (hi, lo) and -f_i are
-// then natural float2 pairs -- 8 pairs of registers each for 16 orbitals,
-// where the source-packed layout needs 16 duplicated pairs -- and only the
+// proxy point).  The per-orbital constants -k log2(e) and -f_i are then
+// natural float2 pairs -- 8 pairs of registers each for 16 orbitals, where
+// the source-packed layout needs 16 duplicated pairs -- and only the
 // source's r, -log2 r and weight are duplicated, once per source for all 16
 // orbitals.  The geometry (differences, r^2, rsqrt, lg2) of two sources is
 // still formed in packed operations and is shared by 16 orbitals: MUFU work
