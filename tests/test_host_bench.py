@@ -68,3 +68,10 @@ def test_cost_model_recovers_near_and_far_costs(bench):
     secs2 = 5e-9 * near - 1e-9 * far
     a2, c2 = bench.cost_model(near, far, secs2)
     assert a2 == c2 == pytest.approx(secs2.sum() / (near + far).sum())
+
+
+def test_loop_variant_follows_the_group_size(bench):
+    assert bench.loop_variant("near_mixed", 1) == 0 and bench.loop_variant("far_mixed", 1) == 1
+    assert bench.loop_variant("near_group", 8) == 2 and bench.loop_variant("far_group", 8) == 3
+    assert bench.loop_variant("near_group", 16) == 4 and bench.loop_variant("far_group", 16) == 5
+    assert bench.loop_variant("near_group", 4) == 2
