@@ -1241,7 +1241,7 @@ def mesh_arm(args):
 
 
 def atom_workload():
-    """BASELINE configs[0]: one Z = 4 nucleus at the origin of [-20, 20]^3, cells of 6^3
+    """The single-atom case: one Z = 4 nucleus at the origin of [-20, 20]^3, cells of 6^3
     first-kind points refined while the centre lies within one cell width of the
     nucleus, depth <= 5 (50,112 points; the literal factor 4 gives 957k points), psi =
     e^{-r}/sqrt(pi), V = -4/sqrt(r^2 + 0.01): the Yukawa call on f = V psi (k = 1) and the

@@ -1,7 +1,7 @@
 // Learned extrapolation of Green iteration: a small MLP on per-cell patches,
 // trained on the device by this file's kernels.  No counterpart in the
 // reference (its closest relative is the Anderson mixing of orbitals,
-// scfFixedPoint.py:491-597); the plain Green-iteration residual judges every
+// scfFixedPoint.py:491-597); the plain Green-iteration residual checks every
 // proposal, so the plain method stays the fallback.
 //
 // Rows are (orbital, cell) patches of P = (order+1)^3 mesh points (the mesh

@@ -7,9 +7,9 @@ predicts the next update d_{t+1} of the patch (in units of the patch's RMS
 update, with a learned skip term alpha d_t).  It is trained online, on the
 device, on the run's own consecutive plain iterates.  A proposal rolls the
 prediction out for a few steps and jumps there; the sweep that follows is the
-judge: if its Green-iteration residual does not fall below the last plain
+check: if its Green-iteration residual does not fall below the last plain
 residual, the jump is undone and the plain iterate continues, so plain Green
-iteration stays both fallback and judge.
+iteration stays both fallback and check.
 
 No counterpart in the reference; the closest is its Anderson mixing of
 (psi, eps) histories (scfFixedPoint.py:491-597).
@@ -310,7 +310,7 @@ class LearnedExtrapolator:
             self.last_res = res
             if len(self.hist) == 3:
                 self._train(gi)
-                # the plain method judges the learner as a whole too: a run in which fewer
+                # the plain method checks the learner as a whole too: a run in which fewer
                 # than a third of the jumps survive stops proposing
                 p = self.stats["proposals"]
                 if p >= 6 and self.stats["accepted"] * 3 < p:

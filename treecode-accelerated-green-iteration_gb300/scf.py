@@ -20,7 +20,7 @@ kernels; the host keeps scalars: occupations (bisection on the Fermi level),
 the Anderson linear system (size <= history), the loop control.
 
 An optional ``extrapolator`` (learned.LearnedExtrapolator) proposes an
-extrapolated orbital set after a sweep; the sweep that follows judges it: a
+extrapolated orbital set after a sweep; the sweep that follows checks it: a
 proposal whose Green-iteration residual is not below the plain iterate's
 previous residual is rolled back, so the plain method stays the fallback.
 """
